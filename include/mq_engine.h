@@ -1,0 +1,120 @@
+/*
+ * mq_engine.h -- C ABI of the GB300 batched ion-trajectory engine.
+ *
+ * Drop-in for the chsim batch engine of filiprumenovski/multiq-workbench: ion states x
+ * operating settings in, per-ion outcome and per-job counts out.  Plain C structs and
+ * pointers only; one engine per host thread; every call is synchronous at the ABI and
+ * returns an mq_status (never aborts).  Status codes are defined in mq_grid.h.
+ *
+ * Reference interfaces replaced (paths inside the reference project):
+ *   mq_engine_create   <- chsim::channel::Engine::new(fields)        simulation/chsim/src/channel.rs:326-340
+ *   mq_engine_destroy  <- Drop of Engine (device buffers, caches)     simulation/chsim/src/channel.rs:309-318
+ *   mq_last_error      <- the panics of Engine (expect/assert text)   simulation/chsim/src/channel.rs:328,331,444,446
+ *   mq_engine_set_dc   <- Engine::dc_buffer (combined DC field)        simulation/chsim/src/channel.rs:383-395
+ *   mq_inject,         <- Engine::inject / mqviz Ion::inject           simulation/chsim/src/channel.rs:342-374,
+ *   mq_inject_grid
+ *                                                                      simulation/mqviz/src/world.rs:407-422
+ *   mq_run_ions        <- Engine::run_batch_ions (states in, states out) simulation/chsim/src/channel.rs:458-475
+ *   mq_run_batch       <- Engine::run_batch (jobs in, Outcome per job)  simulation/chsim/src/channel.rs:437-440
+ *   mq_summarize       <- summarize                                    simulation/chsim/src/channel.rs:496-506
+ *   mq_device_count    <- Device::system_default check                 simulation/chsim/src/channel.rs:328
+ *
+ * Status per ion (chsim): 0 alive, 1 crashed, 2 returned, 3 transmitted, 4 left box, 5 timeout.
+ */
+#ifndef MQ_ENGINE_H
+#define MQ_ENGINE_H
+
+#include "mq_grid.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct mq_engine mq_engine;
+
+#define MQ_PREC_F64   0   /* plain FP64 kernel: bit-exact twin of the FP64 CPU integrator  */
+#define MQ_PREC_MIXED 1   /* batched mixed-precision persistent engine                      */
+
+/* Field grid handed to the engine (caller-owned; copied to the device at create).
+ * Every array holds nx*ny*nz float4 nodes, index i + nx*(j + ny*k) (chsim Fields). */
+typedef struct mq_grid_desc {
+    int32_t nx, ny, nz, pad;
+    double h;                 /* spacing [m]                                         */
+    const float* rf4;         /* RF E per volt, w = conductor mask                   */
+    const float* ac4;         /* AC E per volt                                       */
+    const float* dc4[4];      /* DC bases per volt: Q1, plate, downstream, box (NULL = zero) */
+    double axis_mm;           /* channel axis (x = y)                                */
+    double layers_mm[8];      /* layer boundaries l1..l8 (criteria, crash window)    */
+} mq_grid_desc;
+
+typedef struct mq_species { double mass, z, ccs_n2; } mq_species;        /* Species, channel.rs:235-240 */
+typedef struct mq_rfac { double v_rf, f_rf, v_ac, f_ac; } mq_rfac;       /* RfAc, channel.rs:245-247    */
+typedef struct mq_job { mq_species sp; mq_rfac drive; uint64_t n, seed; } mq_job;   /* Job, channel.rs:250-252 */
+
+/* Physics, channel.rs:254-273, plus the launch distribution. */
+#define MQ_LAUNCH_DISC     0  /* uniform disc r <= r_inject, Maxwell transverse, flux-weighted v_z */
+#define MQ_LAUNCH_LEGACY   1  /* point on axis, 0.1 eV*z*U(0.75,1.5), +-10 deg cone               */
+#define MQ_LAUNCH_GAUSSIAN 2  /* Gaussian spot sigma about the axis, Maxwell velocities          */
+typedef struct mq_physics {
+    int32_t legacy_force, legacy_collisions, legacy_fields, legacy_injection, legacy_criteria;
+    int32_t launch;           /* MQ_LAUNCH_*                                          */
+    int32_t rf_phase0;        /* 1 = RF phase 0 for every ion (chsim convention)       */
+    int32_t pad0;
+    double pressure_pa, temp_k, dt, t_max;
+    double r_inject_mm, sigma_mm, z_inject_mm;
+} mq_physics;
+
+/* Outcome, channel.rs:296-300 */
+typedef struct mq_outcome {
+    uint64_t n, crashed, returned, transmitted, left, timeout;
+    double mean_coll, mean_time;
+} mq_outcome;
+
+/* Caller-owned host ion states, structure of arrays (n entries each). */
+typedef struct mq_ions {
+    double *x, *y, *z, *vx, *vy, *vz;   /* m, m/s                                  */
+    double *ph_rf, *ph_ac;              /* drive phase offsets [cycles]             */
+    uint64_t* rng;                      /* per-ion random state / key               */
+    uint32_t* steps;                    /* executed integrator steps                */
+    uint32_t* ncoll;                    /* accepted collisions                      */
+    int32_t* leg;                       /* legacy: steps to the next collision      */
+    int32_t* status;                    /* chsim status code                        */
+    uint32_t* jid;                      /* job index of each ion                    */
+} mq_ions;
+
+/* Optional per-call measurements. */
+typedef struct mq_run_stats {
+    uint64_t ion_steps;        /* executed ion-steps (sum of step counters)          */
+    double kernel_ms;          /* device time of the whole call (CUDA events)        */
+    uint32_t launches;         /* host-side launch loop iterations / graph replays   */
+    uint32_t kernel_launches;  /* kernels of this library launched by the call       */
+    uint64_t h2d_bytes, d2h_bytes;
+    double step_kernel_ms;     /* device time of the stepping kernel(s) alone        */
+    uint32_t step_kernel_launches;
+    uint32_t pad;
+} mq_run_stats;
+
+int32_t     mq_device_count(void);
+mq_status   mq_engine_create(const mq_grid_desc* grid, int32_t precision, int32_t device, mq_engine** out);
+void        mq_engine_destroy(mq_engine* e);
+const char* mq_last_error(mq_engine* e);
+mq_status   mq_engine_set_dc(mq_engine* e, const double dc[4]);
+/* Injection of every job's ions in job order (n = sum of job.n), on the host. */
+mq_status   mq_inject(mq_engine* e, const mq_job* jobs, size_t njobs, const mq_physics* ph, mq_ions* out, size_t n);
+/* The same injection for a grid without an engine (no device needed). */
+mq_status   mq_inject_grid(const mq_grid_desc* grid, const mq_job* jobs, size_t njobs, const mq_physics* ph,
+                           mq_ions* out, size_t n);
+/* Advance caller states (status 0 ions) by at most max_more steps each (0xFFFFFFFF = to
+ * completion) with the DC field last set; states are read and written in place. */
+mq_status   mq_run_ions(mq_engine* e, const mq_job* jobs, size_t njobs, const mq_physics* ph, mq_ions* io, size_t n,
+                        uint32_t max_more, mq_run_stats* stats);
+/* chsim run_batch: inject (on the device), run every ion to completion, count per job.
+ * out[njobs] receives the outcomes; ions_out (may be NULL) receives final states. */
+mq_status   mq_run_batch(mq_engine* e, const mq_job* jobs, size_t njobs, const double dc[4], const mq_physics* ph,
+                         mq_outcome* out, mq_ions* ions_out, mq_run_stats* stats);
+mq_status   mq_summarize(const mq_ions* io, size_t n, double dt, size_t njobs, mq_outcome* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

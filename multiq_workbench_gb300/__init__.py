@@ -1,0 +1,10 @@
+"""GB300-native batched ion-trajectory engine (drop-in for the chsim batch path of
+filiprumenovski/multiq-workbench).  Public API mirrors chsim: ``Geom``, ``Fields``,
+``Species``, ``RfAc``, ``Job``, ``Physics``, ``Outcome``, ``Engine.run_batch``."""
+from .grid import Geom, Fields, cache_dir, cache_path
+from .channel import (Engine, Species, RfAc, Job, Physics, Outcome, IonStates, RunStats, MqError, summarize, inject,
+                      device_count, PREC_F64, PREC_MIXED, LAUNCH_DISC, LAUNCH_LEGACY, LAUNCH_GAUSSIAN, STATUS)
+
+__all__ = ["Geom", "Fields", "cache_dir", "cache_path", "Engine", "Species", "RfAc", "Job", "Physics", "Outcome",
+           "IonStates", "RunStats", "MqError", "summarize", "inject", "device_count", "PREC_F64", "PREC_MIXED", "LAUNCH_DISC",
+           "LAUNCH_LEGACY", "LAUNCH_GAUSSIAN", "STATUS"]

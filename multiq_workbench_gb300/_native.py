@@ -1,0 +1,169 @@
+"""ctypes view of ``libmqgb.so`` (declarations in include/mq_grid.h and include/mq_engine.h).
+
+The library is built in-tree by :mod:`multiq_workbench_gb300.build`.  Loading fails
+loudly if it is missing: there is no Python or CPU fallback for any engine call.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+_LIB_PATH = Path(__file__).resolve().parent / "libmqgb.so"
+_lib = None
+
+MQ_OK = 0
+MQ_ERRORS = {
+    -1: "invalid argument",
+    -2: "CUDA runtime error",
+    -3: "out of memory",
+    -4: "device watchdog expired",
+    -5: "RF drive must be shared by a batch",
+    -6: "no CUDA device",
+    -7: "Laplace solve did not converge",
+    -8: "request exceeds a fixed capacity",
+}
+
+
+class MqError(RuntimeError):
+    def __init__(self, code: int, what: str, detail: str = ""):
+        self.code = code
+        msg = f"{what}: {MQ_ERRORS.get(code, 'error')} ({code})"
+        if detail:
+            msg += f": {detail}"
+        super().__init__(msg)
+
+
+class mq_geom(C.Structure):
+    _fields_ = [
+        ("de", C.c_double), ("coef", C.c_double), ("q1_start", C.c_double), ("q1_len", C.c_double),
+        ("alpha", C.c_double), ("gap", C.c_double), ("plate", C.c_double), ("hole_d", C.c_double),
+        ("q2_len", C.c_double), ("stem_d", C.c_double), ("q2_flare_bug", C.c_int32), ("tilt_mode", C.c_int32),
+        ("ac_mode", C.c_int32), ("n_xy", C.c_int32), ("grow", C.c_double), ("h_mm", C.c_double),
+        ("mis", C.c_double * 16),
+    ]
+
+
+class mq_solve_stats(C.Structure):
+    _fields_ = [("iterations", C.c_int32), ("converged", C.c_int32), ("final_residual", C.c_double), ("seconds", C.c_double)]
+
+
+class mq_grid_desc(C.Structure):
+    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32), ("pad", C.c_int32), ("h", C.c_double),
+                ("rf4", C.c_void_p), ("ac4", C.c_void_p), ("dc4", C.c_void_p * 4), ("axis_mm", C.c_double),
+                ("layers_mm", C.c_double * 8)]
+
+
+class mq_species(C.Structure):
+    _fields_ = [("mass", C.c_double), ("z", C.c_double), ("ccs_n2", C.c_double)]
+
+
+class mq_rfac(C.Structure):
+    _fields_ = [("v_rf", C.c_double), ("f_rf", C.c_double), ("v_ac", C.c_double), ("f_ac", C.c_double)]
+
+
+class mq_job(C.Structure):
+    _fields_ = [("sp", mq_species), ("drive", mq_rfac), ("n", C.c_uint64), ("seed", C.c_uint64)]
+
+
+class mq_physics(C.Structure):
+    _fields_ = [
+        ("legacy_force", C.c_int32), ("legacy_collisions", C.c_int32), ("legacy_fields", C.c_int32),
+        ("legacy_injection", C.c_int32), ("legacy_criteria", C.c_int32), ("launch", C.c_int32),
+        ("rf_phase0", C.c_int32), ("pad0", C.c_int32),
+        ("pressure_pa", C.c_double), ("temp_k", C.c_double), ("dt", C.c_double), ("t_max", C.c_double),
+        ("r_inject_mm", C.c_double), ("sigma_mm", C.c_double), ("z_inject_mm", C.c_double),
+    ]
+
+
+class mq_outcome(C.Structure):
+    _fields_ = [("n", C.c_uint64), ("crashed", C.c_uint64), ("returned", C.c_uint64), ("transmitted", C.c_uint64),
+                ("left", C.c_uint64), ("timeout", C.c_uint64), ("mean_coll", C.c_double), ("mean_time", C.c_double)]
+
+
+class mq_ions(C.Structure):
+    _fields_ = [("x", C.c_void_p), ("y", C.c_void_p), ("z", C.c_void_p), ("vx", C.c_void_p), ("vy", C.c_void_p),
+                ("vz", C.c_void_p), ("ph_rf", C.c_void_p), ("ph_ac", C.c_void_p), ("rng", C.c_void_p),
+                ("steps", C.c_void_p), ("ncoll", C.c_void_p), ("leg", C.c_void_p), ("status", C.c_void_p),
+                ("jid", C.c_void_p)]
+
+
+class mq_run_stats(C.Structure):
+    _fields_ = [("ion_steps", C.c_uint64), ("kernel_ms", C.c_double), ("launches", C.c_uint32),
+                ("kernel_launches", C.c_uint32), ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64),
+                ("step_kernel_ms", C.c_double), ("step_kernel_launches", C.c_uint32), ("pad", C.c_uint32)]
+
+
+def lib():
+    """The loaded native library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not _LIB_PATH.exists():
+            raise RuntimeError(f"native library missing: {_LIB_PATH} (run multiq_workbench_gb300.build.build())")
+        L = C.CDLL(str(_LIB_PATH))
+        _declare(L)
+        _lib = L
+    return _lib
+
+
+def _declare(L) -> None:
+    P = C.POINTER
+    L.mq_geom_default.argtypes = [P(mq_geom)]
+    L.mq_geom_default.restype = None
+    L.mq_geom_dims.argtypes = [P(mq_geom), P(C.c_int32)]
+    L.mq_geom_dims.restype = C.c_int32
+    L.mq_geom_axis_mm.argtypes = [P(mq_geom)]
+    L.mq_geom_axis_mm.restype = C.c_double
+    L.mq_geom_layers.argtypes = [P(mq_geom), P(C.c_double)]
+    L.mq_geom_layers.restype = None
+    L.mq_geom_classify.argtypes = [P(mq_geom), C.c_void_p, C.c_size_t]
+    L.mq_geom_classify.restype = C.c_int32
+    L.mq_geom_basis_problem.argtypes = [P(mq_geom), C.c_int32, C.c_void_p, C.c_void_p, C.c_size_t, P(C.c_double)]
+    L.mq_geom_basis_problem.restype = C.c_int32
+    L.mq_laplace_solve.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_double, C.c_double,
+                                   C.c_int32, C.c_void_p, P(mq_solve_stats)]
+    L.mq_laplace_solve.restype = C.c_int32
+    L.mq_efield_central.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_void_p]
+    L.mq_efield_central.restype = C.c_int32
+    L.mq_channel_basis.argtypes = [P(mq_geom), C.c_int32, C.c_double, C.c_int32, C.c_void_p, C.c_void_p, P(mq_solve_stats)]
+    L.mq_channel_basis.restype = C.c_int32
+    L.mq_dc_combine.argtypes = [C.c_size_t, C.c_void_p * 4, P(C.c_double), C.c_void_p]
+    L.mq_dc_combine.restype = C.c_int32
+    if hasattr(L, "mq_engine_create"):
+        _declare_engine(L)
+
+
+def _declare_engine(L) -> None:
+    P = C.POINTER
+    L.mq_engine_create.argtypes = [P(mq_grid_desc), C.c_int32, C.c_int32, P(C.c_void_p)]
+    L.mq_engine_create.restype = C.c_int32
+    L.mq_engine_destroy.argtypes = [C.c_void_p]
+    L.mq_engine_destroy.restype = None
+    L.mq_last_error.argtypes = [C.c_void_p]
+    L.mq_last_error.restype = C.c_char_p
+    L.mq_engine_set_dc.argtypes = [C.c_void_p, P(C.c_double)]
+    L.mq_engine_set_dc.restype = C.c_int32
+    L.mq_inject.argtypes = [C.c_void_p, P(mq_job), C.c_size_t, P(mq_physics), P(mq_ions), C.c_size_t]
+    L.mq_inject.restype = C.c_int32
+    L.mq_inject_grid.argtypes = [P(mq_grid_desc), P(mq_job), C.c_size_t, P(mq_physics), P(mq_ions), C.c_size_t]
+    L.mq_inject_grid.restype = C.c_int32
+    L.mq_run_ions.argtypes = [C.c_void_p, P(mq_job), C.c_size_t, P(mq_physics), P(mq_ions), C.c_size_t,
+                              C.c_uint32, P(mq_run_stats)]
+    L.mq_run_ions.restype = C.c_int32
+    L.mq_run_batch.argtypes = [C.c_void_p, P(mq_job), C.c_size_t, P(C.c_double), P(mq_physics), P(mq_outcome),
+                               P(mq_ions), P(mq_run_stats)]
+    L.mq_run_batch.restype = C.c_int32
+    L.mq_summarize.argtypes = [P(mq_ions), C.c_size_t, C.c_double, C.c_size_t, P(mq_outcome)]
+    L.mq_summarize.restype = C.c_int32
+    L.mq_device_count.argtypes = []
+    L.mq_device_count.restype = C.c_int32
+
+
+def check(code: int, what: str, eng=None) -> None:
+    if code != MQ_OK:
+        detail = ""
+        if eng is not None:
+            try:
+                detail = (lib().mq_last_error(eng) or b"").decode()
+            except Exception:
+                detail = ""
+        raise MqError(code, what, detail)

@@ -1,0 +1,550 @@
+// Batched mixed-precision ion-trajectory engine for sm_103a.
+//
+// Same physics as the FP64 integrator (simulation/mqviz/src/world.rs:498-536 with chsim's
+// switches, simulation/chsim/src/channel.metal:70-124), re-shaped for throughput:
+//   * persistent workers: each lane pulls ions from a device work queue (one warp-
+//     aggregated atomic per refill) and advances its ion until it finishes or has done
+//     `chunk` steps; survivors are appended to the next launch's list by warp-ballot
+//     compaction, so every launch starts with dense warps (chsim tc_filter + tc_tail,
+//     channel_tiled.metal:341-482);
+//   * positions in grid units and velocities in cells per step, each an FP32 double-float
+//     (compensated two-sum accumulator); field nodes, interpolation and collision
+//     kinematics in FP32;
+//   * the 8 corners of the ion's cell x {RF, DC, AC} held in registers as trilinear
+//     polynomial coefficients, reloaded only when the ion changes cell (the cached
+//     conductor bits of the corners give the nearest-node crash test);
+//   * RF / AC phase as exact 64-bit fixed-point turn accumulators (phase = offset +
+//     step * f * dt mod 1), evaluated with an FP32 quarter-turn polynomial;
+//   * Philox-4x32-10 counter RNG keyed by the ion's 64-bit key, counter = step.
+#include "mq_mixed.h"
+
+#include <cstring>
+#include <vector>
+
+namespace mqmix {
+namespace {
+
+using mqd::DevGrid;
+using mqd::DevIons;
+
+constexpr unsigned FULL = 0xffffffffu;
+
+struct Ctrs {                       // device counters (32 B)
+    uint32_t head;                  // work-queue head of the current launch
+    uint32_t count[2];              // live-list lengths (ping-pong)
+    uint32_t pad;
+    unsigned long long steps;       // executed ion-steps
+    unsigned long long pad2;
+};
+
+// ---------------------------------------------------------------- Philox-4x32-10
+// Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy as 1, 2, 3" (SC'11).
+__device__ __forceinline__ uint4 philox(uint32_t k0, uint32_t k1, uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        if (r) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
+        uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
+        uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
+        uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+        c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+    }
+    return make_uint4(c0, c1, c2, c3);
+}
+__device__ __forceinline__ float unif(uint32_t x) { return (float)(x >> 8) * 0x1.0p-24f; }
+
+// ---------------------------------------------------------------- FP32 turn-based sine
+// sin / cos Taylor polynomials on [-pi/4, pi/4] (coefficients (-1)^k/(2k+1)!, (-1)^k/(2k)!)
+__device__ __forceinline__ float sinp(float x) {
+    float z = x * x;
+    float p = fmaf(z, 0x1.71de3ap-19f, -0x1.a01a02p-13f);
+    p = fmaf(z, p, 0x1.111112p-7f);
+    p = fmaf(z, p, -0x1.555556p-3f);
+    return fmaf(x * z, p, x);
+}
+__device__ __forceinline__ float cosp(float x) {
+    float z = x * x;
+    float p = fmaf(z, -0x1.27e4fcp-22f, 0x1.a01a02p-16f);
+    p = fmaf(z, p, -0x1.6c16c2p-10f);
+    p = fmaf(z, p, 0x1.555556p-5f);
+    return fmaf(z * z, p, fmaf(z, -0.5f, 1.0f));
+}
+// sin(2 pi P / 2^64) for a 64-bit fixed-point phase in turns
+__device__ __forceinline__ float turn_sin(uint64_t P) {
+    int64_t r = (int64_t)(P << 2);                      // remainder of 4*phase in [-1/2, 1/2) quarter turns
+    uint32_t q = (uint32_t)(P >> 62) + (r < 0 ? 1u : 0u);
+    float x = (float)(int32_t)(r >> 32) * 0x1.921fb6p-32f;   // (pi/2) * 2^-32
+    float s = sinp(x), c = cosp(x);
+    float v = (q & 1u) ? c : s;
+    return (q & 2u) ? -v : v;
+}
+
+// ---------------------------------------------------------------- double-float helpers
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+__device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    e = __fsub_rn(b, __fsub_rn(s, a));
+}
+__device__ __forceinline__ bool df_gt(float h, float l, float th, float tl) { return h > th || (h == th && l > tl); }
+__device__ __forceinline__ bool df_lt(float h, float l, float th, float tl) { return h < th || (h == th && l < tl); }
+
+// ---------------------------------------------------------------- cell cache
+struct Cell {
+    float R[3][8], D[3][8], A[3][8];   // trilinear coefficients per field and component
+    int32_t ci, cj, ck;
+    uint32_t mask;                      // conductor bit per corner (a + 2b + 4c)
+};
+
+__device__ __forceinline__ void to_coef(float f[8], float c[8]) {
+    c[0] = f[0];
+    c[1] = f[1] - f[0];
+    c[2] = f[2] - f[0];
+    c[3] = f[4] - f[0];
+    c[4] = (f[3] - f[1]) - (f[2] - f[0]);
+    c[5] = (f[5] - f[1]) - (f[4] - f[0]);
+    c[6] = (f[6] - f[2]) - (f[4] - f[0]);
+    c[7] = ((f[7] - f[6]) - (f[5] - f[4])) - ((f[3] - f[2]) - (f[1] - f[0]));
+}
+
+__device__ __forceinline__ void load_cell(const DevGrid& g, int32_t ci, int32_t cj, int32_t ck, Cell& c) {
+    const size_t sy = (size_t)g.nx, sz = (size_t)g.nx * (size_t)g.ny;
+    const size_t base = (size_t)ci + sy * (size_t)cj + sz * (size_t)ck;
+    float fr[3][8], fd[3][8], fa[3][8];
+    uint32_t m = 0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        size_t o = base + (size_t)(q & 1) + ((q & 2) ? sy : 0) + ((q & 4) ? sz : 0);
+        float4 r = __ldg(g.rf + o), d = __ldg(g.dc + o), a = __ldg(g.ac + o);
+        fr[0][q] = r.x; fr[1][q] = r.y; fr[2][q] = r.z;
+        fd[0][q] = d.x; fd[1][q] = d.y; fd[2][q] = d.z;
+        fa[0][q] = a.x; fa[1][q] = a.y; fa[2][q] = a.z;
+        m |= (r.w > 0.5f ? 1u : 0u) << q;
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) { to_coef(fr[k], c.R[k]); to_coef(fd[k], c.D[k]); to_coef(fa[k], c.A[k]); }
+    c.ci = ci; c.cj = cj; c.ck = ck; c.mask = m;
+}
+
+__device__ __forceinline__ float tri(const float c[8], float tx, float ty, float tz) {
+    float A = fmaf(tz, c[7], c[4]);
+    float B = fmaf(ty, A, fmaf(tz, c[5], c[1]));
+    float Cc = fmaf(tz, c[6], c[2]);
+    float D = fmaf(tz, c[3], c[0]);
+    return fmaf(tx, B, fmaf(ty, Cc, D));
+}
+
+__device__ __forceinline__ int32_t clampi(int32_t v, int32_t lo, int32_t hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+__device__ __forceinline__ float gauss1(float u1, float u2) {
+    return sqrtf(-2.0f * logf(fmaxf(u1, 0x1.0p-25f))) * cospif(2.0f * u2);
+}
+
+// ---------------------------------------------------------------- the persistent worker
+template <bool LEGACY>
+__global__ void __launch_bounds__(128, 4)
+k_mixed(DevGrid g, MixBatch B, const MixJob* __restrict__ jobs, DevIons io, const uint32_t* __restrict__ list_in,
+        uint32_t* __restrict__ list_out, Ctrs* ctr, int in_slot, uint32_t chunk) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t count = ctr->count[in_slot];
+    if (count == 0) return;
+    uint32_t* count_out = &ctr->count[in_slot ^ 1];
+
+    bool have = false, drained = false;
+    uint32_t id = 0, jid = 0, n = 0, done = 0, ncoll = 0;
+    int32_t leg = 0;
+    float xh[3], xl[3], uh[3], ul[3];
+    uint64_t Prf = 0, Pac = 0, Wac = 0;
+    const uint64_t Wrf = ((uint64_t)B.w_rf_hi << 32) | B.w_rf_lo;
+    float kick = 0.f, v_ac = 0.f, cand_a = 0.f, cand_b = 0.f;
+    uint32_t k0 = 0, k1 = 0;
+    uint4 rc = make_uint4(0, 0, 0, 0);
+    Cell c;
+    unsigned long long steps_total = 0;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) { xh[d] = xl[d] = uh[d] = ul[d] = 0.f; }
+    c.ci = c.cj = c.ck = -1; c.mask = 0;
+
+    for (;;) {
+        // ---- refill: one warp-aggregated atomic hands out queue slots to lanes without an ion
+        const unsigned need = __ballot_sync(FULL, !have && !drained);
+        if (need) {
+            const int leader = __ffs(need) - 1;
+            uint32_t base = 0;
+            if ((int)lane == leader) base = atomicAdd(&ctr->head, (uint32_t)__popc(need));
+            base = __shfl_sync(FULL, base, leader);
+            if (!have && !drained) {
+                const uint32_t slot = base + __popc(need & ((1u << lane) - 1u));
+                if (slot < count) {
+                    id = __ldg(list_in + slot);
+                    jid = io.jid[id];
+                    const MixJob J = jobs[jid];
+                    kick = J.kick; v_ac = J.use_ac ? J.v_ac : 0.0f; cand_a = J.cand_a; cand_b = J.cand_b;
+                    Wac = ((uint64_t)J.w_ac_hi << 32) | J.w_ac_lo;
+                    n = io.steps[id]; ncoll = io.ncoll[id]; leg = io.leg[id];
+                    const double gx[3] = {io.x[id] * B.inv_h, io.y[id] * B.inv_h, io.z[id] * B.inv_h};
+                    const double gu[3] = {io.vx[id] * B.v2u, io.vy[id] * B.v2u, io.vz[id] * B.v2u};
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) {
+                        xh[d] = (float)gx[d]; xl[d] = (float)(gx[d] - (double)xh[d]);
+                        uh[d] = (float)gu[d]; ul[d] = (float)(gu[d] - (double)uh[d]);
+                    }
+                    // phase = offset + n * w (mod 1) in 64-bit fixed point
+                    const double prf = io.ph_rf[id], pac = io.ph_ac[id];
+                    const uint64_t orf = (uint64_t)(prf * 0x1.0p63) << 1, oac = (uint64_t)(pac * 0x1.0p63) << 1;
+                    Prf = orf + (uint64_t)n * Wrf;
+                    Pac = oac + (uint64_t)n * Wac;
+                    const uint64_t key = io.rng[id];
+                    k0 = (uint32_t)key; k1 = (uint32_t)(key >> 32);
+                    rc = philox(k0, k1, n >> 2, 0u, 0u, 0u);
+                    const int32_t ci = clampi(__float2int_rd(xh[0]), 0, B.nx - 2);
+                    const int32_t cj = clampi(__float2int_rd(xh[1]), 0, B.ny - 2);
+                    const int32_t ck = clampi(__float2int_rd(xh[2]), 0, B.nz - 2);
+                    load_cell(g, ci, cj, ck, c);
+                    done = 0;
+                    have = true;
+                } else {
+                    drained = true;
+                }
+            }
+        }
+        if (!__any_sync(FULL, have)) break;
+
+        bool append = false;
+        if (have) {
+            // ---- field at the current position
+            float tx = 0.f, ty = 0.f, tz = 0.f;
+            if (!B.nearest) {
+                tx = __fadd_rn(__fsub_rn(xh[0], (float)c.ci), xl[0]);
+                ty = __fadd_rn(__fsub_rn(xh[1], (float)c.cj), xl[1]);
+                tz = __fadd_rn(__fsub_rn(xh[2], (float)c.ck), xl[2]);
+            }
+            const float a_rf = B.v_rf * turn_sin(Prf);
+            const float a_ac = v_ac * turn_sin(Pac);
+            float E[3];
+#pragma unroll
+            for (int d = 0; d < 3; ++d)
+                E[d] = fmaf(a_rf, tri(c.R[d], tx, ty, tz), fmaf(a_ac, tri(c.A[d], tx, ty, tz), tri(c.D[d], tx, ty, tz)));
+            // ---- kick (compensated) and drift (compensated)
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                float inc = __fadd_rn(__fmul_rn(kick, E[d]), ul[d]);
+                two_sum(uh[d], inc, uh[d], ul[d]);
+                float s, e;
+                fast_two_sum(xh[d], uh[d], s, e);
+                e = __fadd_rn(e, __fadd_rn(xl[d], ul[d]));
+                fast_two_sum(s, e, xh[d], xl[d]);
+            }
+            Prf += Wrf;
+            Pac += Wac;
+            const uint32_t nprev = n;
+            n += 1;
+            done += 1;
+            // ---- collisions
+            if (!LEGACY) {
+                const float u0 = unif((nprev & 3) == 0 ? rc.x : (nprev & 3) == 1 ? rc.y : (nprev & 3) == 2 ? rc.z : rc.w);
+                const float um = sqrtf(fmaf(uh[0], uh[0], fmaf(uh[1], uh[1], uh[2] * uh[2])));
+                if (u0 < fmaf(cand_a, um, cand_b)) {
+                    const MixJob J = jobs[jid];
+                    const uint4 r0 = philox(k0, k1, nprev, 1u, 0u, 0u), r1 = philox(k0, k1, nprev, 1u, 1u, 0u),
+                                r2 = philox(k0, k1, nprev, 1u, 2u, 0u);
+                    const float u2v = (float)B.u2v;
+                    float v[3] = {uh[0] * u2v, uh[1] * u2v, uh[2] * u2v};
+                    const float bound = fmaf(um, u2v, 6.0f * J.s_gas);
+                    float gv[3];
+                    gv[0] = v[0] - J.s_gas * gauss1(unif(r0.x), unif(r0.y));
+                    gv[1] = v[1] - J.s_gas * gauss1(unif(r0.z), unif(r0.w));
+                    gv[2] = v[2] - J.s_gas * gauss1(unif(r1.x), unif(r1.y));
+                    const float gl = sqrtf(fmaf(gv[0], gv[0], fmaf(gv[1], gv[1], gv[2] * gv[2])));
+                    if (unif(r1.z) * bound < gl) {
+                        const float cth = 2.0f * unif(r1.w) - 1.0f;
+                        float sp, cp;
+                        sincospif(2.0f * unif(r2.x), &sp, &cp);
+                        const float sn = sqrtf(fmaxf(0.0f, 1.0f - cth * cth));
+                        const float nn[3] = {sn * cp, sn * sp, cth};
+                        const float v2u = (float)B.v2u;
+#pragma unroll
+                        for (int d = 0; d < 3; ++d) {
+                            float vn = fmaf(J.mr * gl, nn[d], fmaf(-J.mr, gv[d], v[d]));
+                            uh[d] = vn * v2u; ul[d] = 0.0f;
+                        }
+                        ncoll += 1;
+                    }
+                }
+                if ((n & 3) == 0) rc = philox(k0, k1, n >> 2, 0u, 0u, 0u);
+            } else {
+                leg -= 1;
+                if (leg <= 0) {
+                    const MixJob J = jobs[jid];
+                    const uint4 r0 = philox(k0, k1, nprev, 1u, 0u, 0u);
+                    const float u2v = (float)B.u2v;
+                    float v[3] = {uh[0] * u2v, uh[1] * u2v, uh[2] * u2v};
+                    const float vm = sqrtf(fmaf(v[0], v[0], fmaf(v[1], v[1], v[2] * v[2])));
+                    if (vm > J.floor_v) {
+                        const float cth = 2.0f * unif(r0.x) - 1.0f;
+                        float sp, cp;
+                        sincospif(2.0f * unif(r0.y), &sp, &cp);
+                        const float sn = sqrtf(fmaxf(0.0f, 1.0f - cth * cth));
+                        const float dd[3] = {sn * cp, sn * sp, cth};
+                        const float v2u = (float)B.v2u;
+#pragma unroll
+                        for (int d = 0; d < 3; ++d) {
+                            v[d] = fmaf(J.mr * vm, dd[d], v[d] * (1.0f - J.mr));
+                            uh[d] = v[d] * v2u; ul[d] = 0.0f;
+                        }
+                        ncoll += 1;
+                    }
+                    const float mfp = -logf(fmaxf(unif(r0.z), 1e-7f)) * J.mfp_mean;
+                    const float vn = sqrtf(fmaf(v[0], v[0], fmaf(v[1], v[1], v[2] * v[2])));
+                    const float st = floorf(mfp / fmaxf(vn, 1e-3f) / B.dt_f);
+                    leg = st < 1.0f ? 1 : (st < 2147483520.0f ? (int32_t)st : 2147483647);
+                }
+            }
+            // ---- cell of the new position (refresh the cache before the conductor test)
+            const int32_t ci = clampi(__float2int_rd(xh[0]), 0, B.nx - 2);
+            const int32_t cj = clampi(__float2int_rd(xh[1]), 0, B.ny - 2);
+            const int32_t ck = clampi(__float2int_rd(xh[2]), 0, B.nz - 2);
+            if (ci != c.ci || cj != c.cj || ck != c.ck) load_cell(g, ci, cj, ck, c);
+            // ---- termination tests: exit, return, box, conductor, timeout
+            int32_t status = 0;
+            if (df_gt(xh[2], xl[2], B.z_exit_h, B.z_exit_l)) status = 3;
+            else if (df_lt(xh[2], xl[2], B.z_ret_h, B.z_ret_l)) status = 2;
+            else if (df_lt(xh[0], xl[0], 0.f, 0.f) || df_lt(xh[1], xl[1], 0.f, 0.f) || df_lt(xh[2], xl[2], 0.f, 0.f) ||
+                     df_gt(xh[0], xl[0], B.lim_x, 0.f) || df_gt(xh[1], xl[1], B.lim_y, 0.f) || df_gt(xh[2], xl[2], B.lim_z, 0.f))
+                status = 4;
+            else {
+                bool win = df_gt(xh[2], xl[2], B.cz0_h, B.cz0_l) && df_lt(xh[2], xl[2], B.cz1_h, B.cz1_l);
+                if (win) {
+                    const float fx = __fadd_rn(__fsub_rn(xh[0], (float)ci), xl[0]);
+                    const float fy = __fadd_rn(__fsub_rn(xh[1], (float)cj), xl[1]);
+                    const float fz = __fadd_rn(__fsub_rn(xh[2], (float)ck), xl[2]);
+                    const uint32_t q = (fx >= 0.5f ? 1u : 0u) | (fy >= 0.5f ? 2u : 0u) | (fz >= 0.5f ? 4u : 0u);
+                    if ((c.mask >> q) & 1u) status = 1;
+                }
+                if (status == 0 && n >= B.max_steps) status = 5;
+            }
+            if (status != 0 || done >= chunk) {
+                // ---- write back (FP64 state, same layout as the FP64 engine)
+                io.x[id] = ((double)xh[0] + (double)xl[0]) * B.h;
+                io.y[id] = ((double)xh[1] + (double)xl[1]) * B.h;
+                io.z[id] = ((double)xh[2] + (double)xl[2]) * B.h;
+                io.vx[id] = ((double)uh[0] + (double)ul[0]) * B.u2v;
+                io.vy[id] = ((double)uh[1] + (double)ul[1]) * B.u2v;
+                io.vz[id] = ((double)uh[2] + (double)ul[2]) * B.u2v;
+                io.steps[id] = n; io.ncoll[id] = ncoll; io.leg[id] = leg; io.status[id] = status;
+                steps_total += done;
+                append = status == 0;
+                have = false;
+            }
+        }
+        // ---- warp-ballot compaction of survivors into the next launch's list
+        const unsigned am = __ballot_sync(FULL, append);
+        if (am) {
+            const int leader = __ffs(am) - 1;
+            uint32_t base = 0;
+            if ((int)lane == leader) base = atomicAdd(count_out, (uint32_t)__popc(am));
+            base = __shfl_sync(FULL, base, leader);
+            if (append) list_out[base + __popc(am & ((1u << lane) - 1u))] = id;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) steps_total += __shfl_down_sync(FULL, steps_total, o);
+    if (lane == 0 && steps_total) atomicAdd(&ctr->steps, steps_total);
+}
+
+// initial live list: ions with status 0, warp-ballot compaction
+__global__ void k_init_list(DevIons io, uint32_t n, uint32_t* list, Ctrs* ctr) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool live = i < n && io.status[i] == 0;
+    const unsigned m = __ballot_sync(FULL, live);
+    const uint32_t lane = threadIdx.x & 31;
+    if (m) {
+        const int leader = __ffs(m) - 1;
+        uint32_t base = 0;
+        if ((int)lane == leader) base = atomicAdd(&ctr->count[0], (uint32_t)__popc(m));
+        base = __shfl_sync(FULL, base, leader);
+        if (live) list[base + __popc(m & ((1u << lane) - 1u))] = i;
+    }
+}
+
+// prepare launch: clear the queue head and the output count
+__global__ void k_prep(Ctrs* ctr, int out_slot) {
+    ctr->head = 0;
+    ctr->count[out_slot] = 0;
+}
+
+void split(double v, float& h, float& l) {
+    h = (float)v;
+    l = (float)(v - (double)h);
+}
+
+uint64_t fix64(double turns_per_step) {   // round(frac(w) * 2^64)
+    double f = turns_per_step - floor(turns_per_step);
+    long double s = (long double)f * 18446744073709551616.0L;
+    long double r = floorl(s + 0.5L);
+    if (r >= 18446744073709551616.0L) return 0;
+    return (uint64_t)r;
+}
+
+}  // namespace
+
+MixJob make_mix_job(const mqp::JobC& j, const mqp::Batch& b) {
+    MixJob m;
+    std::memset(&m, 0, sizeof(m));
+    m.kick = (float)(j.qmdt * b.dt / b.h);
+    m.v_ac = (float)j.v_ac;
+    m.cand_a = (float)(j.nsd * b.h / b.dt);
+    m.cand_b = (float)(j.nsd * 6.0 * j.s_gas);
+    m.s_gas = (float)j.s_gas;
+    m.mr = (float)j.mr;
+    m.floor_v = (float)j.floor_v;
+    m.mfp_mean = (float)j.mfp_mean;
+    uint64_t w = fix64(j.w_ac);
+    m.w_ac_lo = (uint32_t)w;
+    m.w_ac_hi = (uint32_t)(w >> 32);
+    m.use_ac = j.use_ac;
+    return m;
+}
+
+MixBatch make_mix_batch(const mqp::Batch& b) {
+    MixBatch m;
+    std::memset(&m, 0, sizeof(m));
+    m.h = b.h;
+    m.inv_h = 1.0 / b.h;
+    m.dt = b.dt;
+    m.u2v = b.h / b.dt;
+    m.v2u = b.dt / b.h;
+    m.v_rf = (float)b.v_rf;
+    m.dt_f = (float)b.dt;
+    uint64_t w = fix64(b.w_rf);
+    m.w_rf_lo = (uint32_t)w;
+    m.w_rf_hi = (uint32_t)(w >> 32);
+    split(b.z_exit / b.h, m.z_exit_h, m.z_exit_l);
+    split(b.z_return / b.h, m.z_ret_h, m.z_ret_l);
+    split(b.crash_z0 / b.h, m.cz0_h, m.cz0_l);
+    split(b.crash_z1 / b.h, m.cz1_h, m.cz1_l);
+    m.lim_x = (float)(b.nx - 1);
+    m.lim_y = (float)(b.ny - 1);
+    m.lim_z = (float)(b.nz - 1);
+    m.nx = b.nx; m.ny = b.ny; m.nz = b.nz;
+    m.nearest = b.nearest;
+    m.legacy_coll = b.legacy_coll;
+    m.max_steps = b.max_steps;
+    return m;
+}
+
+Tuning default_tuning(int device) {
+    Tuning t;
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) { cudaGetLastError(); sms = 1; }
+    t.sms = sms;
+    return t;
+}
+
+void release(Scratch& s) {
+    if (s.graph) cudaGraphExecDestroy(s.graph);
+    for (void* p : {s.lists, s.ctrs, s.params, s.jobs}) if (p) cudaFree(p);
+    for (auto& e : s.ev) if (e) cudaEventDestroy(e);
+    s = Scratch();
+}
+
+static cudaError_t enqueue_launches(const Scratch& s, const Tuning& t, DevGrid g, const MixBatch& mb, DevIons io,
+                                    uint32_t n, uint32_t launches, uint32_t chunk, uint32_t last_chunk, cudaStream_t st,
+                                    uint32_t* kernels) {
+    uint32_t* lists = static_cast<uint32_t*>(s.lists);
+    Ctrs* ctr = static_cast<Ctrs*>(s.ctrs);
+    const MixJob* jobs = static_cast<const MixJob*>(s.jobs);
+    const int grid = t.sms * t.blocks_per_sm;
+    for (uint32_t L = 0; L < launches; ++L) {
+        const int in = (int)(L & 1);
+        k_prep<<<1, 1, 0, st>>>(ctr, in ^ 1);
+        const uint32_t ch = (L + 1 == launches) ? last_chunk : chunk;
+        if (mb.legacy_coll)
+            k_mixed<true><<<grid, t.tpb, 0, st>>>(g, mb, jobs, io, lists + (size_t)in * n, lists + (size_t)(in ^ 1) * n, ctr, in, ch);
+        else
+            k_mixed<false><<<grid, t.tpb, 0, st>>>(g, mb, jobs, io, lists + (size_t)in * n, lists + (size_t)(in ^ 1) * n, ctr, in, ch);
+        *kernels += 2;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t run(Scratch& s, const Tuning& t, DevGrid g, const mqp::Batch& b, const MixJob* jobs, size_t njobs,
+                DevIons io, uint32_t n, uint32_t max_more, cudaStream_t st, RunInfo* info) {
+    cudaError_t e;
+    *info = RunInfo();
+    if (n == 0) return cudaSuccess;
+    if (t.tpb != 128) return cudaErrorInvalidValue;   // the kernel is compiled for 128-thread blocks
+    const size_t list_bytes = (size_t)2 * n * sizeof(uint32_t);
+    if (s.list_cap < list_bytes) {
+        if (s.lists) cudaFree(s.lists);
+        s.lists = nullptr; s.list_cap = 0;
+        if ((e = cudaMalloc(&s.lists, list_bytes)) != cudaSuccess) return e;
+        s.list_cap = list_bytes;
+    }
+    if (!s.ctrs && (e = cudaMalloc(&s.ctrs, sizeof(Ctrs))) != cudaSuccess) return e;
+    if (s.jobs_cap < njobs * sizeof(MixJob)) {
+        if (s.jobs) cudaFree(s.jobs);
+        s.jobs = nullptr; s.jobs_cap = 0;
+        if ((e = cudaMalloc(&s.jobs, njobs * sizeof(MixJob))) != cudaSuccess) return e;
+        s.jobs_cap = njobs * sizeof(MixJob);
+    }
+    if (!s.ev[0]) { cudaEventCreate(&s.ev[0]); cudaEventCreate(&s.ev[1]); }
+    if ((e = cudaMemcpyAsync(s.jobs, jobs, njobs * sizeof(MixJob), cudaMemcpyHostToDevice, st)) != cudaSuccess) return e;
+    const MixBatch mb = make_mix_batch(b);
+    // launches needed: every live ion has at most min(max_more, max_steps) steps left
+    const uint64_t need = max_more < b.max_steps ? (uint64_t)max_more : (uint64_t)b.max_steps;
+    const uint32_t chunk = t.chunk ? t.chunk : 4096;
+    uint32_t launches = (uint32_t)((need + chunk - 1) / chunk);
+    if (launches == 0) launches = 1;
+    const uint32_t last_chunk = (uint32_t)(need - (uint64_t)(launches - 1) * chunk) ? (uint32_t)(need - (uint64_t)(launches - 1) * chunk) : chunk;
+    Ctrs* ctr = static_cast<Ctrs*>(s.ctrs);
+    if ((e = cudaMemsetAsync(ctr, 0, sizeof(Ctrs), st)) != cudaSuccess) return e;
+    k_init_list<<<(n + 255) / 256, 256, 0, st>>>(io, n, static_cast<uint32_t*>(s.lists), ctr);
+    info->kernel_launches += 1;
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    cudaEventRecord(s.ev[0], st);
+    uint32_t kernels = 0;
+    const bool graph = t.use_graph && launches > 1;
+    if (graph) {
+        const uint64_t key[6] = {(uint64_t)(uintptr_t)s.lists, (uint64_t)n, launches, ((uint64_t)chunk << 32) | last_chunk,
+                                 (uint64_t)(uintptr_t)io.x ^ ((uint64_t)t.blocks_per_sm << 56), (uint64_t)(uintptr_t)g.dc};
+        cudaGraph_t gr = nullptr;
+        if ((e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return e;
+        enqueue_launches(s, t, g, mb, io, n, launches, chunk, last_chunk, st, &kernels);
+        e = cudaStreamEndCapture(st, &gr);
+        if (e != cudaSuccess) { if (gr) cudaGraphDestroy(gr); return e; }
+        // re-use the instantiated graph when only kernel parameters changed
+        bool updated = false;
+        if (s.graph && std::memcmp(key, s.graph_key, sizeof(key)) == 0) {
+            cudaGraphExecUpdateResultInfo ri;
+            if (cudaGraphExecUpdate(s.graph, gr, &ri) == cudaSuccess) updated = true;
+            else cudaGetLastError();
+        }
+        if (!updated) {
+            if (s.graph) { cudaGraphExecDestroy(s.graph); s.graph = nullptr; }
+            if ((e = cudaGraphInstantiate(&s.graph, gr, 0)) != cudaSuccess) { cudaGraphDestroy(gr); return e; }
+            std::memcpy(s.graph_key, key, sizeof(key));
+        }
+        cudaGraphDestroy(gr);
+        if ((e = cudaGraphLaunch(s.graph, st)) != cudaSuccess) return e;
+        info->graph_replays = 1;
+    } else {
+        if ((e = enqueue_launches(s, t, g, mb, io, n, launches, chunk, last_chunk, st, &kernels)) != cudaSuccess) return e;
+    }
+    cudaEventRecord(s.ev[1], st);
+    Ctrs h;
+    if ((e = cudaMemcpyAsync(&h, ctr, sizeof(Ctrs), cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+    cudaEventElapsedTime(&info->step_ms, s.ev[0], s.ev[1]);
+    info->ion_steps = h.steps;
+    info->step_launches = launches;
+    info->kernel_launches += kernels;
+    // after the last launch the surviving list must be empty unless the step budget ran out
+    const uint32_t survivors = h.count[launches & 1];
+    info->watchdog = (survivors != 0 && max_more >= b.max_steps) ? 1 : 0;
+    return cudaSuccess;
+}
+
+}  // namespace mqmix

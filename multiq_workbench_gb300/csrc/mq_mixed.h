@@ -1,0 +1,74 @@
+// Mixed-precision batched engine (internal interface; see mq_mixed.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "mq_internal.h"
+
+namespace mqmix {
+
+// Per-job constants of the mixed kernel.  Positions are held in grid units (cells) and
+// velocities in cells per step, so the kick is E [V/m] * qm_kick * dt^2 / h.
+struct MixJob {
+    float kick;        // qm_kick * dt * dt / h
+    float v_ac;        // AC amplitude [V]
+    float cand_a;      // null-collision candidate probability per |u| (nsd * h / dt)
+    float cand_b;      //   ... constant part (nsd * 6 s_gas)
+    float s_gas;       // Maxwell gas std [m/s]
+    float mr;          // M_gas / (m + M_gas)
+    float floor_v;     // legacy: no collision below this speed [m/s]; < 0 = thermal gas
+    float mfp_mean;    // legacy mean free path [m]
+    uint32_t w_ac_lo, w_ac_hi;   // AC phase increment per step, turns * 2^64
+    int32_t use_ac;
+    int32_t pad;
+};
+
+struct MixBatch {      // per-batch constants (device-resident parameter block)
+    double h, inv_h, dt, u2v, v2u;   // u2v = h / dt (cells/step -> m/s)
+    float v_rf, dt_f;
+    uint32_t w_rf_lo, w_rf_hi;       // RF phase increment per step, turns * 2^64
+    float z_exit_h, z_exit_l, z_ret_h, z_ret_l;       // grid units, double-float
+    float cz0_h, cz0_l, cz1_h, cz1_l;                 // crash window, grid units
+    float lim_x, lim_y, lim_z;                        // n - 1 (exact)
+    int32_t nx, ny, nz;
+    int32_t nearest, legacy_coll;
+    uint32_t max_steps;
+    int32_t pad;
+};
+
+struct Tuning {
+    int tpb = 128;             // threads per block
+    int blocks_per_sm = 4;     // resident blocks per SM for the persistent grid
+    uint32_t chunk = 4096;     // steps per ion per launch (compaction interval)
+    int use_graph = 1;         // replay the launch sequence as one CUDA graph
+    int sms = 0;               // filled from the device
+};
+
+struct Scratch {
+    void* lists = nullptr;     // two live-ion lists (ping-pong), u32 each
+    size_t list_cap = 0;
+    void* ctrs = nullptr;      // counters: [0] head, [1..2] counts, [4..5] steps (u64), ...
+    void* params = nullptr;    // MixBatch
+    void* jobs = nullptr;      // MixJob[]
+    size_t jobs_cap = 0;
+    cudaGraphExec_t graph = nullptr;
+    uint64_t graph_key[6] = {0, 0, 0, 0, 0, 0};
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+};
+
+struct RunInfo {
+    uint64_t ion_steps = 0;
+    float step_ms = 0.0f;
+    uint32_t step_launches = 0;
+    uint32_t kernel_launches = 0;
+    uint32_t graph_replays = 0;
+    int watchdog = 0;
+};
+
+MixJob make_mix_job(const mqp::JobC& j, const mqp::Batch& b);
+MixBatch make_mix_batch(const mqp::Batch& b);
+Tuning default_tuning(int device);
+cudaError_t run(Scratch& s, const Tuning& t, mqd::DevGrid g, const mqp::Batch& b, const MixJob* jobs, size_t njobs,
+                mqd::DevIons io, uint32_t n, uint32_t max_more, cudaStream_t st, RunInfo* info);
+void release(Scratch& s);
+
+}  // namespace mqmix
