@@ -1,0 +1,324 @@
+"""Benchmark: ion-steps/s of the batched mixed-precision engine on one GB300.
+
+Workload (the batched sweep): 64 excitation frequencies (80-120 kHz, linear) x 8 excitation
+amplitudes (0.1-1.0 V) x 32 m/z (470-532, step 2; z = +1, mass = m/z, N2 CCS = 2.95 m^(2/3))
+x 256 ions = 4,194,304 ions in 16,384 jobs sharing one RF drive (100 V, 500 kHz), on the
+channel geometry solved at 0.100 mm (160 x 160 x 242 nodes), DC [Q1 0, plate +5, down -5,
+box 0] V, 1 mTorr N2 at 300 K, Gaussian launch sigma 0.1 mm at z = 1 mm with 300 K
+Maxwell velocities, dt = 100 ns, at most 20,000 steps, legacy half-kick update rule.
+Synthetic inputs (seeded); nothing is read from a dataset.
+
+One bench step = one Engine.run_batch of that whole batch (device injection, the persistent
+stepping kernel to completion, per-job counts).  ``value`` is device time (CUDA events on
+the engine's stream); ``e2e`` is wall time of the public call with host-side jobs in and
+outcomes out.  L2 is flushed (256 MB write) before every timed step.
+
+``--impl reference`` times the reference's CPU algorithm (the FP64 C restatement under
+oracle/) on the host cores for the same workload and metric, on a bounded sample.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "ion-steps/s, 1 GB300: batched mixed-precision vs plain FP64 at matched outcomes"
+UNIT = "ion-steps/s"
+BYTES_PER_ION_STEP = 384   # 8 corner nodes x 3 float4 fields (RF+mask, DC, AC) x 16 B
+
+
+def workload(ions_per_job: int = 256, seed0: int = 0):
+    import multiq_workbench_gb300 as mq
+    fac = np.linspace(80e3, 120e3, 64)
+    vac = np.linspace(0.1, 1.0, 8)
+    mzs = [470.0 + 2 * k for k in range(32)]
+    jobs = []
+    for a in fac:
+        for v in vac:
+            for m in mzs:
+                jobs.append(mq.Job(mq.Species(m, 1.0, 2.95 * m ** (2.0 / 3.0)), mq.RfAc(100.0, 500e3, float(v), float(a)),
+                                   ions_per_job, seed0 + len(jobs)))
+    ph = mq.Physics(legacy_force=True, pressure_pa=0.133322, temp_k=300.0, dt=1e-7, t_max=20000 * 1e-7,
+                    launch=mq.LAUNCH_GAUSSIAN, sigma_mm=0.1, z_inject_mm=1.0)
+    return jobs, ph, [0.0, 5.0, -5.0, 0.0]
+
+
+def fields():
+    import multiq_workbench_gb300 as mq
+    return mq.Fields.build(mq.Geom(), bases=[0, 1, 3, 4])
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int = 0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm = [float(r[1]) for r in self.rows if len(r) >= 9 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) >= 9 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            if len(r) >= 9:
+                for k, nm in enumerate(names):
+                    if r[5 + k].lower().startswith("active"):
+                        reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except ValueError:
+            pass
+    return {}
+
+
+def cpu_rate(jobs, ph, dc, f, sample_jobs: int, threads: int, target_s: float | None = None) -> dict:
+    """The FP64 CPU restatement of the reference integrator on a bounded sample of the batch:
+    ``sample_jobs`` evenly spaced jobs, run to completion.  With ``target_s`` the sample is
+    first sized so that the timed run takes about that long."""
+    from oracle import mqref as R
+    g = f.geom
+    dcf = f.dc_field(dc)
+    G = R.Grid3(f.nx, f.ny, f.nz, f.h, f.rf, f.ac, dcf)
+
+    def one(k: int):
+        step = max(1, len(jobs) // k)
+        js = jobs[::step][:k]
+        b = R.batch(ph, js[0].drive.v_rf, js[0].drive.f_rf, g.axis(), g.layers())
+        n = sum(j.n for j in js)
+        s = R.inject(b, js, n)
+        t0 = time.perf_counter()
+        steps = R.run(G, b, js, s, threads=threads)
+        return steps, time.perf_counter() - t0, n, len(js)
+
+    k = sample_jobs
+    if target_s:
+        steps, dt, _, _ = one(k)
+        k = int(min(len(jobs), max(k, k * target_s / max(dt, 1e-3))))
+    steps, dt, n, nj = one(k)
+    return {"value": steps / dt, "steps": steps, "seconds": dt, "ions": n, "jobs": nj}
+
+
+def flush_l2(buf):
+    buf.fill_(1)
+
+
+def run_reference(args, rank: int, world: int):
+    if rank != 0:
+        return
+    jobs, ph, dc = workload()
+    f = fields()
+    threads = os.cpu_count() or 1
+    vals = []
+    # size one step to ~10 s of CPU work; warm-up steps run a small sample untimed
+    probe = cpu_rate(jobs, ph, dc, f, 128, threads)
+    sample = int(min(len(jobs), max(128, 128 * 10.0 / max(probe["seconds"], 1e-3))))
+    for _ in range(max(0, args.warmup)):
+        cpu_rate(jobs, ph, dc, f, 64, threads)
+    r = None
+    t_all = time.perf_counter()
+    for _ in range(args.steps):
+        r = cpu_rate(jobs, ph, dc, f, sample, threads)
+        vals.append(r["value"])
+    wall = time.perf_counter() - t_all
+    v = float(np.median(vals))
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * wall / max(1, args.steps), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "batched sweep 64 f_ac x 8 V_ac x 32 m/z x 256 ions (4,194,304 ions), 0.100 mm grid, legacy half-kick",
+                       "sample": f"{r['jobs']} of 16384 jobs (every {len(jobs) // r['jobs']}th), {r['ions']} ions per step"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{r['ions']} ions of {r['jobs']} evenly spaced jobs, run to completion"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-f64", action="store_true", help="skip the FP64 comparison leg")
+    ap.add_argument("--no-tune", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if args.impl == "gb300" else "gloo")
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        if dist:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+
+    import torch
+    import __graft_entry__ as ge
+    import multiq_workbench_gb300 as mq
+
+    ge.build()
+    torch.cuda.set_device(local)
+    jobs, ph, dc = workload(seed0=rank * 1_000_003)
+    f = fields()
+    eng = mq.Engine(f, mq.PREC_MIXED, device=local)
+    tuned = None
+    if not args.no_tune:
+        tuned, _ = eng.autotune(jobs, dc, ph, sample_per_job=64)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+
+    for _ in range(args.warmup):
+        eng.run_batch(jobs, dc, ph)
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    clocks.start()
+    dev_ms, step_ms, steps_total, launches, walls = [], [], 0, 0, []
+    h2d = d2h = 0
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    for _ in range(args.steps):
+        flush_l2(flush)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = eng.run_batch(jobs, dc, ph)
+        walls.append(time.perf_counter() - t0)
+        s = eng.last_stats
+        dev_ms.append(s.kernel_ms)
+        step_ms.append(s.step_kernel_ms)
+        steps_total += s.ion_steps
+        launches += s.kernel_launches
+        h2d, d2h = s.h2d_bytes, s.d2h_bytes
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    t_dev = sum(dev_ms) * 1e-3
+    t_wall = sum(walls)
+    if dist:
+        tt = torch.tensor([t_dev, t_wall], dtype=torch.float64, device=f"cuda:{local}")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        st = torch.tensor([float(steps_total)], dtype=torch.float64, device=f"cuda:{local}")
+        dist.all_reduce(st, op=dist.ReduceOp.SUM)
+        t_dev, t_wall, steps_all = float(tt[0]), float(tt[1]), float(st[0])
+    else:
+        steps_all = float(steps_total)
+    value = steps_all / t_dev
+    e2e_value = steps_all / t_wall
+    counts = {k: int(sum(getattr(o, k) for o in out)) for k in ("transmitted", "returned", "crashed", "left", "timeout")}
+
+    extra = {}
+    if rank == 0 and not args.no_f64:
+        # FP64 kernel vs mixed engine on the same 1/16 sample (16 ions of every job): speed and outcomes
+        sj = [mq.Job(j.sp, j.drive, 16, j.seed) for j in jobs]
+        with mq.Engine(f, mq.PREC_F64, device=local) as e64:
+            o64 = e64.run_batch(sj, dc, ph)
+            s64 = e64.last_stats
+        om = eng.run_batch(sj, dc, ph)
+        sm = eng.last_stats
+        pulls = {}
+        for k in ("transmitted", "returned", "crashed", "timeout"):
+            a = sum(getattr(o, k) for o in om)
+            b = sum(getattr(o, k) for o in o64)
+            n = sum(o.n for o in o64)
+            p = (a + b + 1) / (2 * n + 2)
+            pulls[k] = {"mixed": a, "fp64": b, "pull": (a - b) / math.sqrt(2 * n * p * (1 - p))}
+        extra["fp64_gpu"] = {"value": s64.ion_steps / (s64.kernel_ms * 1e-3), "unit": UNIT,
+                             "mixed_same_sample": sm.ion_steps / (sm.kernel_ms * 1e-3),
+                             "speedup_mixed_over_fp64": (sm.ion_steps / sm.kernel_ms) / (s64.ion_steps / s64.kernel_ms),
+                             "sample": f"{sum(j.n for j in sj)} ions (16 of each job)", "outcomes": pulls}
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        r = cpu_rate(jobs, ph, dc, f, 128, os.cpu_count() or 1, target_s=12.0)
+        cpu = {"value": r["value"], "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+               "sample": f"{r['ions']} ions of {r['jobs']} evenly spaced jobs run to completion ({r['seconds']:.1f} s)"}
+
+    peaks = measured_peaks()
+    hbm = peaks.get("hbm_gbs")
+    peak_src = "measured" if hbm else "fallback"
+    hbm = hbm or 6800.0
+    kern_s = sum(step_ms) * 1e-3
+    achieved = BYTES_PER_ION_STEP * steps_total / kern_s / 1e9
+    # DRAM bytes of one k_mixed launch from the committed ncu summary of this workload
+    prof = ROOT / "profiles" / "k_mixed_batched_sweep.md"
+    traffic = None
+    if prof.exists():
+        import re
+        m = re.search(r"dram_bytes_per_launch:\s*([0-9.eE+]+)", prof.read_text())
+        traffic = float(m.group(1)) if m else None
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+                "config": {"workload": "batched sweep 64 f_ac x 8 V_ac x 32 m/z x 256 ions (4,194,304 ions), "
+                                       "0.100 mm channel grid 160x160x242, legacy half-kick, <=20000 steps",
+                           "jobs": len(jobs), "ions": sum(j.n for j in jobs), "l2_flush": "256 MB write before every timed step",
+                           "tuning": tuned or eng.tuning()},
+                "ion_steps_per_step": steps_total / args.steps,
+                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+                "gpu_launches": int(launches),
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                             "traffic": traffic, "peak_source": f"{peak_src} hbm_gbs",
+                             "kernel": "k_mixed", "algorithmic_bytes_per_ion_step": BYTES_PER_ION_STEP},
+                "cpu_baseline": cpu, "clocks": clk, "outcomes": counts}
+        line.update(extra)
+        print(json.dumps(line), flush=True)
+    eng.close()
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

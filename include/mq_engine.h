@@ -114,6 +114,22 @@ mq_status   mq_run_batch(mq_engine* e, const mq_job* jobs, size_t njobs, const d
                          mq_outcome* out, mq_ions* ions_out, mq_run_stats* stats);
 mq_status   mq_summarize(const mq_ions* io, size_t n, double dt, size_t njobs, mq_outcome* out);
 
+/* Launch shape of the mixed engine (no counterpart in the reference, whose worker shape is
+ * fixed by #defines and environment variables: simulation/chsim/src/tiled.rs:10-29). */
+typedef struct mq_tuning {
+    int32_t threads_per_block;   /* fixed at 128                                          */
+    int32_t blocks_per_sm;       /* resident blocks per SM of the persistent grid (1..3)   */
+    uint32_t chunk;              /* steps per ion per launch (compaction interval)         */
+    int32_t use_graph;           /* replay the launch sequence as one CUDA graph           */
+} mq_tuning;
+mq_status   mq_engine_get_tuning(mq_engine* e, mq_tuning* t);
+mq_status   mq_engine_set_tuning(mq_engine* e, const mq_tuning* t);
+/* Autotuner: times every candidate shape on a sample of the batch (the first
+ * sample_per_job ions of each job), keeps the fastest as the engine's tuning and returns
+ * it with its rate in ion-steps/s.  Mixed engine only. */
+mq_status   mq_engine_autotune(mq_engine* e, const mq_job* jobs, size_t njobs, const double dc[4], const mq_physics* ph,
+                               uint64_t sample_per_job, mq_tuning* best, double* best_rate);
+
 #ifdef __cplusplus
 }
 #endif

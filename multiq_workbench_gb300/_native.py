@@ -93,6 +93,11 @@ class mq_run_stats(C.Structure):
                 ("step_kernel_ms", C.c_double), ("step_kernel_launches", C.c_uint32), ("pad", C.c_uint32)]
 
 
+class mq_tuning(C.Structure):
+    _fields_ = [("threads_per_block", C.c_int32), ("blocks_per_sm", C.c_int32), ("chunk", C.c_uint32),
+                ("use_graph", C.c_int32)]
+
+
 def lib():
     """The loaded native library (raises if it has not been built)."""
     global _lib
@@ -156,6 +161,13 @@ def _declare_engine(L) -> None:
     L.mq_summarize.restype = C.c_int32
     L.mq_device_count.argtypes = []
     L.mq_device_count.restype = C.c_int32
+    L.mq_engine_get_tuning.argtypes = [C.c_void_p, P(mq_tuning)]
+    L.mq_engine_get_tuning.restype = C.c_int32
+    L.mq_engine_set_tuning.argtypes = [C.c_void_p, P(mq_tuning)]
+    L.mq_engine_set_tuning.restype = C.c_int32
+    L.mq_engine_autotune.argtypes = [C.c_void_p, P(mq_job), C.c_size_t, P(C.c_double), P(mq_physics), C.c_uint64,
+                                     P(mq_tuning), P(C.c_double)]
+    L.mq_engine_autotune.restype = C.c_int32
 
 
 def check(code: int, what: str, eng=None) -> None:

@@ -233,6 +233,28 @@ class Engine:
     def __exit__(self, *a):
         self.close()
 
+    def tuning(self) -> dict:
+        t = N.mq_tuning()
+        N.check(N.lib().mq_engine_get_tuning(self._h, C.byref(t)), "mq_engine_get_tuning", self._h)
+        return dict(threads_per_block=t.threads_per_block, blocks_per_sm=t.blocks_per_sm, chunk=t.chunk,
+                    use_graph=bool(t.use_graph))
+
+    def set_tuning(self, blocks_per_sm: int | None = None, chunk: int | None = None, use_graph: bool | None = None) -> None:
+        cur = self.tuning()
+        t = N.mq_tuning(128, int(blocks_per_sm if blocks_per_sm is not None else cur["blocks_per_sm"]),
+                        int(chunk if chunk is not None else cur["chunk"]),
+                        int(use_graph if use_graph is not None else cur["use_graph"]))
+        N.check(N.lib().mq_engine_set_tuning(self._h, C.byref(t)), "mq_engine_set_tuning", self._h)
+
+    def autotune(self, jobs, dc, ph: Physics, sample_per_job: int = 2048) -> tuple[dict, float]:
+        """Time candidate launch shapes on a sample of the batch and keep the fastest."""
+        t = N.mq_tuning()
+        rate = C.c_double(0.0)
+        v = (C.c_double * 4)(*[float(x) for x in dc])
+        N.check(N.lib().mq_engine_autotune(self._h, jobs_native(jobs), len(jobs), v, C.byref(ph.native()),
+                                           int(sample_per_job), C.byref(t), C.byref(rate)), "mq_engine_autotune", self._h)
+        return self.tuning(), float(rate.value)
+
     def set_dc(self, dc) -> None:
         v = (C.c_double * 4)(*[float(x) for x in dc])
         N.check(N.lib().mq_engine_set_dc(self._h, v), "mq_engine_set_dc", self._h)

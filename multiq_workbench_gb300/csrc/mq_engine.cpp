@@ -49,6 +49,7 @@ struct mq_engine {
     float4* d_dcb[4] = {nullptr, nullptr, nullptr, nullptr};
     double dc_cur[4] = {0, 0, 0, 0};
     bool dc_valid = false;
+    uint64_t grid_gen = 0;         // bumped whenever the combined DC field changes
     cudaStream_t st = nullptr;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     DevBuf ions[14];
@@ -283,8 +284,8 @@ mq_status run_mixed(mq_engine* e, const mq_job* jobs, size_t njobs, const mq_phy
     std::vector<mqmix::MixJob> mj(njobs);
     for (size_t k = 0; k < njobs; ++k) mj[k] = mqmix::make_mix_job(make_job(jobs[k], ph), b);
     mqmix::RunInfo info;
-    cudaError_t c = mqmix::run(e->mix, e->tune, dev_grid(e), b, mj.data(), njobs, dev_ions(e), (uint32_t)n, max_more,
-                               e->st, &info);
+    cudaError_t c = mqmix::run(e->mix, e->tune, dev_grid(e), e->grid_gen, b, mj.data(), njobs, dev_ions(e), (uint32_t)n,
+                               max_more, e->st, &info);
     if (c != cudaSuccess) return cuda_fail(e, c, "mixed engine");
     if (info.watchdog) return fail(e, MQ_ERR_WATCHDOG, "mixed engine: launch budget exhausted with live ions");
     *steps_out = info.ion_steps;
@@ -363,6 +364,7 @@ mq_status mq_engine_set_dc(mq_engine* e, const double dc[4]) {
     CK(cudaStreamSynchronize(e->st), "DC combine kernel");
     std::memcpy(e->dc_cur, dc, sizeof(e->dc_cur));
     e->dc_valid = true;
+    e->grid_gen += 1;
     return MQ_OK;
 }
 
@@ -497,6 +499,58 @@ mq_status mq_run_batch(mq_engine* e, const mq_job* jobs, size_t njobs, const dou
         stats->d2h_bytes = d2h;
         stats->kernel_launches += (uint32_t)ntab + 2;   // phase tables + inject + summary
     }
+    return MQ_OK;
+}
+
+mq_status mq_engine_get_tuning(mq_engine* e, mq_tuning* t) {
+    if (!e || !t) return MQ_ERR_INVALID;
+    t->threads_per_block = e->tune.tpb;
+    t->blocks_per_sm = e->tune.blocks_per_sm;
+    t->chunk = e->tune.chunk;
+    t->use_graph = e->tune.use_graph;
+    return MQ_OK;
+}
+
+mq_status mq_engine_set_tuning(mq_engine* e, const mq_tuning* t) {
+    if (!e || !t) return MQ_ERR_INVALID;
+    if (t->threads_per_block != 128 || t->blocks_per_sm < 1 || t->blocks_per_sm > 3 || t->chunk == 0)
+        return fail(e, MQ_ERR_INVALID, "tuning: 128 threads per block, 1..3 blocks per SM, chunk > 0");
+    e->tune.tpb = t->threads_per_block;
+    e->tune.blocks_per_sm = t->blocks_per_sm;
+    e->tune.chunk = t->chunk;
+    e->tune.use_graph = t->use_graph ? 1 : 0;
+    return MQ_OK;
+}
+
+mq_status mq_engine_autotune(mq_engine* e, const mq_job* jobs, size_t njobs, const double dc[4], const mq_physics* ph,
+                             uint64_t sample_per_job, mq_tuning* best, double* best_rate) {
+    mq_status s = check_batch(e, jobs, njobs, ph);
+    if (s != MQ_OK) return s;
+    if (e->prec != MQ_PREC_MIXED) return fail(e, MQ_ERR_INVALID, "the autotuner shapes the mixed engine");
+    if (sample_per_job == 0) return fail(e, MQ_ERR_INVALID, "sample_per_job must be > 0");
+    std::vector<mq_job> sj(jobs, jobs + njobs);
+    for (auto& j : sj) j.n = j.n < sample_per_job ? j.n : sample_per_job;
+    std::vector<mq_outcome> out(njobs);
+    const mqmix::Tuning keep = e->tune;
+    mqmix::Tuning top = keep;
+    double top_rate = -1.0;
+    const int blocks[] = {2, 3};
+    const uint32_t chunks[] = {1024, 2048, 4096, 8192, 20000};
+    for (int bl : blocks)
+        for (uint32_t ch : chunks) {
+            e->tune = keep;
+            e->tune.blocks_per_sm = bl;
+            e->tune.chunk = ch;
+            mq_run_stats st;
+            // first call warms the graph and caches; the second is timed
+            if ((s = mq_run_batch(e, sj.data(), njobs, dc, ph, out.data(), nullptr, &st)) != MQ_OK) { e->tune = keep; return s; }
+            if ((s = mq_run_batch(e, sj.data(), njobs, dc, ph, out.data(), nullptr, &st)) != MQ_OK) { e->tune = keep; return s; }
+            double rate = st.step_kernel_ms > 0 ? (double)st.ion_steps / (st.step_kernel_ms * 1e-3) : 0.0;
+            if (rate > top_rate) { top_rate = rate; top = e->tune; }
+        }
+    e->tune = top;
+    if (best) mq_engine_get_tuning(e, best);
+    if (best_rate) *best_rate = top_rate;
     return MQ_OK;
 }
 

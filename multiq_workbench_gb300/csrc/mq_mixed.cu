@@ -10,9 +10,10 @@
 //   * positions in grid units and velocities in cells per step, each an FP32 double-float
 //     (compensated two-sum accumulator); field nodes, interpolation and collision
 //     kinematics in FP32;
-//   * the 8 corners of the ion's cell x {RF, DC, AC} held in registers as trilinear
-//     polynomial coefficients, reloaded only when the ion changes cell (the cached
-//     conductor bits of the corners give the nearest-node crash test);
+//   * fields as 48-byte interleaved node records; the 8 corners of the ion's cell x
+//     {RF, DC, AC} held in registers and reloaded only when the ion changes cell (the
+//     cached conductor bits of the corners give the nearest-node crash test), with an L1
+//     prefetch of the cell the ion is heading for;
 //   * RF / AC phase as exact 64-bit fixed-point turn accumulators (phase = offset +
 //     step * f * dt mod 1), evaluated with an FP32 quarter-turn polynomial;
 //   * Philox-4x32-10 counter RNG keyed by the ion's 64-bit key, counter = step.
@@ -92,61 +93,67 @@ __device__ __forceinline__ bool df_gt(float h, float l, float th, float tl) { re
 __device__ __forceinline__ bool df_lt(float h, float l, float th, float tl) { return h < th || (h == th && l < tl); }
 
 // ---------------------------------------------------------------- cell cache
+// Interleaved node records: node q occupies float4 [3q] = {RF.xyz, conductor mask},
+// [3q+1] = {combined DC.xyz, 0}, [3q+2] = {AC.xyz, 0} (48 B), so the 8 corners of a cell are
+// 4 runs of 96 contiguous bytes.
 struct Cell {
-    float R[3][8], D[3][8], A[3][8];   // trilinear coefficients per field and component
+    float R[3][8], D[3][8], A[3][8];   // corner values per field and component, corner q = a + 2b + 4c
     int32_t ci, cj, ck;
-    uint32_t mask;                      // conductor bit per corner (a + 2b + 4c)
+    uint32_t mask;                      // conductor bit per corner
 };
 
-__device__ __forceinline__ void to_coef(float f[8], float c[8]) {
-    c[0] = f[0];
-    c[1] = f[1] - f[0];
-    c[2] = f[2] - f[0];
-    c[3] = f[4] - f[0];
-    c[4] = (f[3] - f[1]) - (f[2] - f[0]);
-    c[5] = (f[5] - f[1]) - (f[4] - f[0]);
-    c[6] = (f[6] - f[2]) - (f[4] - f[0]);
-    c[7] = ((f[7] - f[6]) - (f[5] - f[4])) - ((f[3] - f[2]) - (f[1] - f[0]));
+__device__ __forceinline__ size_t node_of(const MixBatch& B, int32_t ci, int32_t cj, int32_t ck) {
+    return (size_t)ci + (size_t)B.nx * ((size_t)cj + (size_t)B.ny * (size_t)ck);
 }
 
-__device__ __forceinline__ void load_cell(const DevGrid& g, int32_t ci, int32_t cj, int32_t ck, Cell& c) {
-    const size_t sy = (size_t)g.nx, sz = (size_t)g.nx * (size_t)g.ny;
-    const size_t base = (size_t)ci + sy * (size_t)cj + sz * (size_t)ck;
-    float fr[3][8], fd[3][8], fa[3][8];
+__device__ __forceinline__ void load_cell(const float4* __restrict__ nodes, const MixBatch& B, int32_t ci, int32_t cj,
+                                          int32_t ck, Cell& c) {
+    const size_t sy = (size_t)B.nx, sz = (size_t)B.nx * (size_t)B.ny;
+    const size_t base = node_of(B, ci, cj, ck);
     uint32_t m = 0;
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
-        size_t o = base + (size_t)(q & 1) + ((q & 2) ? sy : 0) + ((q & 4) ? sz : 0);
-        float4 r = __ldg(g.rf + o), d = __ldg(g.dc + o), a = __ldg(g.ac + o);
-        fr[0][q] = r.x; fr[1][q] = r.y; fr[2][q] = r.z;
-        fd[0][q] = d.x; fd[1][q] = d.y; fd[2][q] = d.z;
-        fa[0][q] = a.x; fa[1][q] = a.y; fa[2][q] = a.z;
+        const size_t o = 3 * (base + (size_t)(q & 1) + ((q & 2) ? sy : 0) + ((q & 4) ? sz : 0));
+        const float4 r = __ldg(nodes + o), d = __ldg(nodes + o + 1), a = __ldg(nodes + o + 2);
+        c.R[0][q] = r.x; c.R[1][q] = r.y; c.R[2][q] = r.z;
+        c.D[0][q] = d.x; c.D[1][q] = d.y; c.D[2][q] = d.z;
+        c.A[0][q] = a.x; c.A[1][q] = a.y; c.A[2][q] = a.z;
         m |= (r.w > 0.5f ? 1u : 0u) << q;
     }
-#pragma unroll
-    for (int k = 0; k < 3; ++k) { to_coef(fr[k], c.R[k]); to_coef(fd[k], c.D[k]); to_coef(fa[k], c.A[k]); }
     c.ci = ci; c.cj = cj; c.ck = ck; c.mask = m;
 }
 
-__device__ __forceinline__ float tri(const float c[8], float tx, float ty, float tz) {
-    float A = fmaf(tz, c[7], c[4]);
-    float B = fmaf(ty, A, fmaf(tz, c[5], c[1]));
-    float Cc = fmaf(tz, c[6], c[2]);
-    float D = fmaf(tz, c[3], c[0]);
-    return fmaf(tx, B, fmaf(ty, Cc, D));
+// pull the 4 corner runs of a cell into L1 ahead of use
+__device__ __forceinline__ void prefetch_cell(const float4* nodes, const MixBatch& B, int32_t ci, int32_t cj, int32_t ck) {
+    const size_t sy = (size_t)B.nx, sz = (size_t)B.nx * (size_t)B.ny;
+    const size_t base = node_of(B, ci, cj, ck);
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        const float4* p = nodes + 3 * (base + ((r & 1) ? sy : 0) + ((r & 2) ? sz : 0));
+        asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+        asm volatile("prefetch.global.L1 [%0];" ::"l"(p + 5));
+    }
+}
+
+// E = a_rf RF(t) + DC(t) + a_ac AC(t): corner values combined first, then one trilinear pass
+__device__ __forceinline__ float field_comp(const float R[8], const float D[8], const float A[8], float a_rf, float a_ac,
+                                            float tx, float ty, float tz) {
+    float F[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) F[q] = fmaf(a_rf, R[q], fmaf(a_ac, A[q], D[q]));
+    const float c00 = fmaf(tx, F[1] - F[0], F[0]), c10 = fmaf(tx, F[3] - F[2], F[2]);
+    const float c01 = fmaf(tx, F[5] - F[4], F[4]), c11 = fmaf(tx, F[7] - F[6], F[6]);
+    const float c0 = fmaf(ty, c10 - c00, c00), c1 = fmaf(ty, c11 - c01, c01);
+    return fmaf(tz, c1 - c0, c0);
 }
 
 __device__ __forceinline__ int32_t clampi(int32_t v, int32_t lo, int32_t hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
-__device__ __forceinline__ float gauss1(float u1, float u2) {
-    return sqrtf(-2.0f * logf(fmaxf(u1, 0x1.0p-25f))) * cospif(2.0f * u2);
-}
-
 // ---------------------------------------------------------------- the persistent worker
 template <bool LEGACY>
-__global__ void __launch_bounds__(128, 4)
-k_mixed(DevGrid g, MixBatch B, const MixJob* __restrict__ jobs, DevIons io, const uint32_t* __restrict__ list_in,
-        uint32_t* __restrict__ list_out, Ctrs* ctr, int in_slot, uint32_t chunk) {
+__global__ void __launch_bounds__(128, 3)
+k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__ jobs, DevIons io,
+        const uint32_t* __restrict__ list_in, uint32_t* __restrict__ list_out, Ctrs* ctr, int in_slot, uint32_t chunk) {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t count = ctr->count[in_slot];
     if (count == 0) return;
@@ -160,7 +167,11 @@ k_mixed(DevGrid g, MixBatch B, const MixJob* __restrict__ jobs, DevIons io, cons
     const uint64_t Wrf = ((uint64_t)B.w_rf_hi << 32) | B.w_rf_lo;
     float kick = 0.f, v_ac = 0.f, cand_a = 0.f, cand_b = 0.f;
     uint32_t k0 = 0, k1 = 0;
-    uint4 rc = make_uint4(0, 0, 0, 0);
+    // per-step candidate uniforms: Philox block n>>2 (rc) and the next block (rn); rn is
+    // refreshed for every lane on a warp-uniform schedule (every 4 loop iterations), so the
+    // 10-round generator runs with all lanes active instead of once per lane-boundary
+    uint4 rc = make_uint4(0, 0, 0, 0), rn = make_uint4(0, 0, 0, 0);
+    uint32_t iter = 0;
     Cell c;
     unsigned long long steps_total = 0;
 #pragma unroll
@@ -198,11 +209,9 @@ k_mixed(DevGrid g, MixBatch B, const MixJob* __restrict__ jobs, DevIons io, cons
                     Pac = oac + (uint64_t)n * Wac;
                     const uint64_t key = io.rng[id];
                     k0 = (uint32_t)key; k1 = (uint32_t)(key >> 32);
-                    rc = philox(k0, k1, n >> 2, 0u, 0u, 0u);
-                    const int32_t ci = clampi(__float2int_rd(xh[0]), 0, B.nx - 2);
-                    const int32_t cj = clampi(__float2int_rd(xh[1]), 0, B.ny - 2);
-                    const int32_t ck = clampi(__float2int_rd(xh[2]), 0, B.nz - 2);
-                    load_cell(g, ci, cj, ck, c);
+                    if (!LEGACY) { rc = philox(k0, k1, n >> 2, 0u, 0u, 0u); rn = philox(k0, k1, (n >> 2) + 1u, 0u, 0u, 0u); }
+                    load_cell(nodes, B, clampi(__float2int_rd(xh[0]), 0, B.nx - 2), clampi(__float2int_rd(xh[1]), 0, B.ny - 2),
+                              clampi(__float2int_rd(xh[2]), 0, B.nz - 2), c);
                     done = 0;
                     have = true;
                 } else {
@@ -213,6 +222,8 @@ k_mixed(DevGrid g, MixBatch B, const MixJob* __restrict__ jobs, DevIons io, cons
         if (!__any_sync(FULL, have)) break;
 
         bool append = false;
+        if (!LEGACY && (iter & 3u) == 0u && have) rn = philox(k0, k1, (n >> 2) + 1u, 0u, 0u, 0u);
+        ++iter;
         if (have) {
             // ---- field at the current position
             float tx = 0.f, ty = 0.f, tz = 0.f;
@@ -225,8 +236,7 @@ k_mixed(DevGrid g, MixBatch B, const MixJob* __restrict__ jobs, DevIons io, cons
             const float a_ac = v_ac * turn_sin(Pac);
             float E[3];
 #pragma unroll
-            for (int d = 0; d < 3; ++d)
-                E[d] = fmaf(a_rf, tri(c.R[d], tx, ty, tz), fmaf(a_ac, tri(c.A[d], tx, ty, tz), tri(c.D[d], tx, ty, tz)));
+            for (int d = 0; d < 3; ++d) E[d] = field_comp(c.R[d], c.D[d], c.A[d], a_rf, a_ac, tx, ty, tz);
             // ---- kick (compensated) and drift (compensated)
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
@@ -248,23 +258,29 @@ k_mixed(DevGrid g, MixBatch B, const MixJob* __restrict__ jobs, DevIons io, cons
                 const float um = sqrtf(fmaf(uh[0], uh[0], fmaf(uh[1], uh[1], uh[2] * uh[2])));
                 if (u0 < fmaf(cand_a, um, cand_b)) {
                     const MixJob J = jobs[jid];
-                    const uint4 r0 = philox(k0, k1, nprev, 1u, 0u, 0u), r1 = philox(k0, k1, nprev, 1u, 1u, 0u),
-                                r2 = philox(k0, k1, nprev, 1u, 2u, 0u);
-                    const float u2v = (float)B.u2v;
+                    // gas velocity: three normals from four uniforms (two Box-Muller radii);
+                    // acceptance and the isotropic direction from a second block
+                    const uint4 r0 = philox(k0, k1, nprev, 1u, 0u, 0u), r1 = philox(k0, k1, nprev, 1u, 1u, 0u);
+                    const float u2v = B.u2v_f;
                     float v[3] = {uh[0] * u2v, uh[1] * u2v, uh[2] * u2v};
                     const float bound = fmaf(um, u2v, 6.0f * J.s_gas);
+                    const float g1 = sqrtf(-2.0f * logf(fmaxf(unif(r0.x), 0x1.0p-25f)));
+                    const float g2 = sqrtf(-2.0f * logf(fmaxf(unif(r0.z), 0x1.0p-25f)));
+                    float s1, c1;
+                    sincospif(2.0f * unif(r0.y), &s1, &c1);
+                    const float c2 = cospif(2.0f * unif(r0.w));
                     float gv[3];
-                    gv[0] = v[0] - J.s_gas * gauss1(unif(r0.x), unif(r0.y));
-                    gv[1] = v[1] - J.s_gas * gauss1(unif(r0.z), unif(r0.w));
-                    gv[2] = v[2] - J.s_gas * gauss1(unif(r1.x), unif(r1.y));
+                    gv[0] = fmaf(-J.s_gas, g1 * c1, v[0]);
+                    gv[1] = fmaf(-J.s_gas, g1 * s1, v[1]);
+                    gv[2] = fmaf(-J.s_gas, g2 * c2, v[2]);
                     const float gl = sqrtf(fmaf(gv[0], gv[0], fmaf(gv[1], gv[1], gv[2] * gv[2])));
-                    if (unif(r1.z) * bound < gl) {
-                        const float cth = 2.0f * unif(r1.w) - 1.0f;
+                    if (unif(r1.x) * bound < gl) {
+                        const float cth = 2.0f * unif(r1.y) - 1.0f;
                         float sp, cp;
-                        sincospif(2.0f * unif(r2.x), &sp, &cp);
+                        sincospif(2.0f * unif(r1.z), &sp, &cp);
                         const float sn = sqrtf(fmaxf(0.0f, 1.0f - cth * cth));
                         const float nn[3] = {sn * cp, sn * sp, cth};
-                        const float v2u = (float)B.v2u;
+                        const float v2u = B.v2u_f;
 #pragma unroll
                         for (int d = 0; d < 3; ++d) {
                             float vn = fmaf(J.mr * gl, nn[d], fmaf(-J.mr, gv[d], v[d]));
@@ -273,13 +289,13 @@ k_mixed(DevGrid g, MixBatch B, const MixJob* __restrict__ jobs, DevIons io, cons
                         ncoll += 1;
                     }
                 }
-                if ((n & 3) == 0) rc = philox(k0, k1, n >> 2, 0u, 0u, 0u);
+                if ((n & 3) == 0) rc = rn;   // rn holds block n>>2: refreshed at most 3 iterations ago
             } else {
                 leg -= 1;
                 if (leg <= 0) {
                     const MixJob J = jobs[jid];
                     const uint4 r0 = philox(k0, k1, nprev, 1u, 0u, 0u);
-                    const float u2v = (float)B.u2v;
+                    const float u2v = B.u2v_f;
                     float v[3] = {uh[0] * u2v, uh[1] * u2v, uh[2] * u2v};
                     const float vm = sqrtf(fmaf(v[0], v[0], fmaf(v[1], v[1], v[2] * v[2])));
                     if (vm > J.floor_v) {
@@ -288,7 +304,7 @@ k_mixed(DevGrid g, MixBatch B, const MixJob* __restrict__ jobs, DevIons io, cons
                         sincospif(2.0f * unif(r0.y), &sp, &cp);
                         const float sn = sqrtf(fmaxf(0.0f, 1.0f - cth * cth));
                         const float dd[3] = {sn * cp, sn * sp, cth};
-                        const float v2u = (float)B.v2u;
+                        const float v2u = B.v2u_f;
 #pragma unroll
                         for (int d = 0; d < 3; ++d) {
                             v[d] = fmaf(J.mr * vm, dd[d], v[d] * (1.0f - J.mr));
@@ -302,11 +318,18 @@ k_mixed(DevGrid g, MixBatch B, const MixJob* __restrict__ jobs, DevIons io, cons
                     leg = st < 1.0f ? 1 : (st < 2147483520.0f ? (int32_t)st : 2147483647);
                 }
             }
-            // ---- cell of the new position (refresh the cache before the conductor test)
+            // ---- cell of the new position (refresh the cache before the conductor test), and
+            //      an L1 prefetch of the cell one more step ahead
             const int32_t ci = clampi(__float2int_rd(xh[0]), 0, B.nx - 2);
             const int32_t cj = clampi(__float2int_rd(xh[1]), 0, B.ny - 2);
             const int32_t ck = clampi(__float2int_rd(xh[2]), 0, B.nz - 2);
-            if (ci != c.ci || cj != c.cj || ck != c.ck) load_cell(g, ci, cj, ck, c);
+            if (ci != c.ci || cj != c.cj || ck != c.ck) load_cell(nodes, B, ci, cj, ck, c);
+            {
+                const int32_t pi = clampi(__float2int_rd(xh[0] + uh[0]), 0, B.nx - 2);
+                const int32_t pj = clampi(__float2int_rd(xh[1] + uh[1]), 0, B.ny - 2);
+                const int32_t pk = clampi(__float2int_rd(xh[2] + uh[2]), 0, B.nz - 2);
+                if (pi != ci || pj != cj || pk != ck) prefetch_cell(nodes, B, pi, pj, pk);
+            }
             // ---- termination tests: exit, return, box, conductor, timeout
             int32_t status = 0;
             if (df_gt(xh[2], xl[2], B.z_exit_h, B.z_exit_l)) status = 3;
@@ -315,8 +338,7 @@ k_mixed(DevGrid g, MixBatch B, const MixJob* __restrict__ jobs, DevIons io, cons
                      df_gt(xh[0], xl[0], B.lim_x, 0.f) || df_gt(xh[1], xl[1], B.lim_y, 0.f) || df_gt(xh[2], xl[2], B.lim_z, 0.f))
                 status = 4;
             else {
-                bool win = df_gt(xh[2], xl[2], B.cz0_h, B.cz0_l) && df_lt(xh[2], xl[2], B.cz1_h, B.cz1_l);
-                if (win) {
+                if (df_gt(xh[2], xl[2], B.cz0_h, B.cz0_l) && df_lt(xh[2], xl[2], B.cz1_h, B.cz1_l)) {
                     const float fx = __fadd_rn(__fsub_rn(xh[0], (float)ci), xl[0]);
                     const float fy = __fadd_rn(__fsub_rn(xh[1], (float)cj), xl[1]);
                     const float fz = __fadd_rn(__fsub_rn(xh[2], (float)ck), xl[2]);
@@ -352,6 +374,16 @@ k_mixed(DevGrid g, MixBatch B, const MixJob* __restrict__ jobs, DevIons io, cons
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) steps_total += __shfl_down_sync(FULL, steps_total, o);
     if (lane == 0 && steps_total) atomicAdd(&ctr->steps, steps_total);
+}
+
+// interleave RF | combined DC | AC into 48-byte node records (once per DC configuration)
+__global__ void k_pack_nodes(const float4* __restrict__ rf, const float4* __restrict__ dc, const float4* __restrict__ ac,
+                             float4* __restrict__ nodes, size_t n) {
+    const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    nodes[3 * q] = rf[q];
+    nodes[3 * q + 1] = dc[q];
+    nodes[3 * q + 2] = ac[q];
 }
 
 // initial live list: ions with status 0, warp-ballot compaction
@@ -418,6 +450,8 @@ MixBatch make_mix_batch(const mqp::Batch& b) {
     m.v2u = b.dt / b.h;
     m.v_rf = (float)b.v_rf;
     m.dt_f = (float)b.dt;
+    m.u2v_f = (float)m.u2v;
+    m.v2u_f = (float)m.v2u;
     uint64_t w = fix64(b.w_rf);
     m.w_rf_lo = (uint32_t)w;
     m.w_rf_hi = (uint32_t)(w >> 32);
@@ -445,37 +479,57 @@ Tuning default_tuning(int device) {
 
 void release(Scratch& s) {
     if (s.graph) cudaGraphExecDestroy(s.graph);
-    for (void* p : {s.lists, s.ctrs, s.params, s.jobs}) if (p) cudaFree(p);
+    for (void* p : {s.lists, s.ctrs, s.params, s.jobs, s.nodes}) if (p) cudaFree(p);
     for (auto& e : s.ev) if (e) cudaEventDestroy(e);
     s = Scratch();
 }
 
-static cudaError_t enqueue_launches(const Scratch& s, const Tuning& t, DevGrid g, const MixBatch& mb, DevIons io,
+static cudaError_t enqueue_launches(const Scratch& s, const Tuning& t, const MixBatch& mb, DevIons io,
                                     uint32_t n, uint32_t launches, uint32_t chunk, uint32_t last_chunk, cudaStream_t st,
                                     uint32_t* kernels) {
     uint32_t* lists = static_cast<uint32_t*>(s.lists);
     Ctrs* ctr = static_cast<Ctrs*>(s.ctrs);
     const MixJob* jobs = static_cast<const MixJob*>(s.jobs);
+    const float4* nodes = static_cast<const float4*>(s.nodes);
     const int grid = t.sms * t.blocks_per_sm;
     for (uint32_t L = 0; L < launches; ++L) {
         const int in = (int)(L & 1);
         k_prep<<<1, 1, 0, st>>>(ctr, in ^ 1);
         const uint32_t ch = (L + 1 == launches) ? last_chunk : chunk;
         if (mb.legacy_coll)
-            k_mixed<true><<<grid, t.tpb, 0, st>>>(g, mb, jobs, io, lists + (size_t)in * n, lists + (size_t)(in ^ 1) * n, ctr, in, ch);
+            k_mixed<true><<<grid, t.tpb, 0, st>>>(nodes, mb, jobs, io, lists + (size_t)in * n, lists + (size_t)(in ^ 1) * n, ctr, in, ch);
         else
-            k_mixed<false><<<grid, t.tpb, 0, st>>>(g, mb, jobs, io, lists + (size_t)in * n, lists + (size_t)(in ^ 1) * n, ctr, in, ch);
+            k_mixed<false><<<grid, t.tpb, 0, st>>>(nodes, mb, jobs, io, lists + (size_t)in * n, lists + (size_t)(in ^ 1) * n, ctr, in, ch);
         *kernels += 2;
     }
     return cudaGetLastError();
 }
 
-cudaError_t run(Scratch& s, const Tuning& t, DevGrid g, const mqp::Batch& b, const MixJob* jobs, size_t njobs,
-                DevIons io, uint32_t n, uint32_t max_more, cudaStream_t st, RunInfo* info) {
+cudaError_t pack_nodes(Scratch& s, DevGrid g, uint64_t grid_gen, cudaStream_t st, uint32_t* kernels) {
+    if (s.nodes && s.nodes_gen == grid_gen) return cudaSuccess;
+    cudaError_t e;
+    const size_t n = (size_t)g.nx * g.ny * g.nz;
+    const size_t bytes = 3 * n * sizeof(float4);
+    if (s.nodes_cap < bytes) {
+        if (s.nodes) cudaFree(s.nodes);
+        s.nodes = nullptr; s.nodes_cap = 0;
+        if ((e = cudaMalloc(&s.nodes, bytes)) != cudaSuccess) return e;
+        s.nodes_cap = bytes;
+    }
+    k_pack_nodes<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(g.rf, g.dc, g.ac, static_cast<float4*>(s.nodes), n);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    *kernels += 1;
+    s.nodes_gen = grid_gen;
+    return cudaSuccess;
+}
+
+cudaError_t run(Scratch& s, const Tuning& t, DevGrid g, uint64_t grid_gen, const mqp::Batch& b, const MixJob* jobs,
+                size_t njobs, DevIons io, uint32_t n, uint32_t max_more, cudaStream_t st, RunInfo* info) {
     cudaError_t e;
     *info = RunInfo();
     if (n == 0) return cudaSuccess;
     if (t.tpb != 128) return cudaErrorInvalidValue;   // the kernel is compiled for 128-thread blocks
+    if ((e = pack_nodes(s, g, grid_gen, st, &info->kernel_launches)) != cudaSuccess) return e;
     const size_t list_bytes = (size_t)2 * n * sizeof(uint32_t);
     if (s.list_cap < list_bytes) {
         if (s.lists) cudaFree(s.lists);
@@ -509,10 +563,10 @@ cudaError_t run(Scratch& s, const Tuning& t, DevGrid g, const mqp::Batch& b, con
     const bool graph = t.use_graph && launches > 1;
     if (graph) {
         const uint64_t key[6] = {(uint64_t)(uintptr_t)s.lists, (uint64_t)n, launches, ((uint64_t)chunk << 32) | last_chunk,
-                                 (uint64_t)(uintptr_t)io.x ^ ((uint64_t)t.blocks_per_sm << 56), (uint64_t)(uintptr_t)g.dc};
+                                 (uint64_t)(uintptr_t)io.x ^ ((uint64_t)t.blocks_per_sm << 56), (uint64_t)(uintptr_t)s.nodes};
         cudaGraph_t gr = nullptr;
         if ((e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return e;
-        enqueue_launches(s, t, g, mb, io, n, launches, chunk, last_chunk, st, &kernels);
+        enqueue_launches(s, t, mb, io, n, launches, chunk, last_chunk, st, &kernels);
         e = cudaStreamEndCapture(st, &gr);
         if (e != cudaSuccess) { if (gr) cudaGraphDestroy(gr); return e; }
         // re-use the instantiated graph when only kernel parameters changed
@@ -531,7 +585,7 @@ cudaError_t run(Scratch& s, const Tuning& t, DevGrid g, const mqp::Batch& b, con
         if ((e = cudaGraphLaunch(s.graph, st)) != cudaSuccess) return e;
         info->graph_replays = 1;
     } else {
-        if ((e = enqueue_launches(s, t, g, mb, io, n, launches, chunk, last_chunk, st, &kernels)) != cudaSuccess) return e;
+        if ((e = enqueue_launches(s, t, mb, io, n, launches, chunk, last_chunk, st, &kernels)) != cudaSuccess) return e;
     }
     cudaEventRecord(s.ev[1], st);
     Ctrs h;

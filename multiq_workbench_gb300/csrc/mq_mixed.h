@@ -24,7 +24,7 @@ struct MixJob {
 
 struct MixBatch {      // per-batch constants (device-resident parameter block)
     double h, inv_h, dt, u2v, v2u;   // u2v = h / dt (cells/step -> m/s)
-    float v_rf, dt_f;
+    float v_rf, dt_f, u2v_f, v2u_f;
     uint32_t w_rf_lo, w_rf_hi;       // RF phase increment per step, turns * 2^64
     float z_exit_h, z_exit_l, z_ret_h, z_ret_l;       // grid units, double-float
     float cz0_h, cz0_l, cz1_h, cz1_l;                 // crash window, grid units
@@ -50,6 +50,9 @@ struct Scratch {
     void* params = nullptr;    // MixBatch
     void* jobs = nullptr;      // MixJob[]
     size_t jobs_cap = 0;
+    void* nodes = nullptr;     // interleaved RF | DC | AC node records (float4 x 3 per node)
+    size_t nodes_cap = 0;
+    uint64_t nodes_gen = ~0ull; // grid generation the records were packed from
     cudaGraphExec_t graph = nullptr;
     uint64_t graph_key[6] = {0, 0, 0, 0, 0, 0};
     cudaEvent_t ev[2] = {nullptr, nullptr};
@@ -67,8 +70,8 @@ struct RunInfo {
 MixJob make_mix_job(const mqp::JobC& j, const mqp::Batch& b);
 MixBatch make_mix_batch(const mqp::Batch& b);
 Tuning default_tuning(int device);
-cudaError_t run(Scratch& s, const Tuning& t, mqd::DevGrid g, const mqp::Batch& b, const MixJob* jobs, size_t njobs,
-                mqd::DevIons io, uint32_t n, uint32_t max_more, cudaStream_t st, RunInfo* info);
+cudaError_t run(Scratch& s, const Tuning& t, mqd::DevGrid g, uint64_t grid_gen, const mqp::Batch& b, const MixJob* jobs,
+                size_t njobs, mqd::DevIons io, uint32_t n, uint32_t max_more, cudaStream_t st, RunInfo* info);
 void release(Scratch& s);
 
 }  // namespace mqmix

@@ -1,0 +1,103 @@
+"""Host-side logic without a GPU: injection parity with the oracle, physics presets, the C
+ABI's exported symbols and its refusal paths, and job sharding across ranks."""
+import ctypes as C
+import os
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+@pytest.mark.parametrize("launch,legacy,rf0", [(0, False, True), (1, True, True), (2, False, False), (2, False, True)])
+def test_host_injection_equals_oracle(coarse, launch, legacy, rf0):
+    import multiq_workbench_gb300 as mq
+    from oracle import mqref as R
+    ph = mq.Physics(legacy_collisions=legacy, legacy_injection=legacy, pressure_pa=0.133322, dt=1e-7, t_max=1e-3,
+                    r_inject_mm=2.0, launch=launch, sigma_mm=0.1, rf_phase0=rf0)
+    jobs = [mq.Job(mq.Species(499.0 * z, z, 185.6 if z == 1 else 0.0), mq.RfAc(100.0, 500e3, 0.5, 1e5), 300, 17 + int(z))
+            for z in (1.0, 5.0)]
+    ions = mq.inject(coarse, jobs, ph)
+    g = coarse.geom
+    s = R.inject(R.batch(ph, 100.0, 500e3, g.axis(), g.layers()), jobs, 600)
+    for k, _ in R.FIELDS:
+        assert np.array_equal(getattr(ions, k).view(np.uint8), getattr(s, k).view(np.uint8)), k
+    if launch == 2:
+        r = np.hypot(ions.x - g.axis() * 1e-3, ions.y - g.axis() * 1e-3)
+        assert 0.08e-3 < np.sqrt((r ** 2).mean() / 2) < 0.12e-3       # sigma 0.1 mm per axis
+    if rf0:
+        assert (ions.ph_rf == 0).all()
+
+
+def test_physics_presets_follow_chsim(monkeypatch):
+    import multiq_workbench_gb300 as mq
+    leg = mq.Physics.legacy(0.1333)
+    assert (leg.legacy_force, leg.legacy_collisions, leg.legacy_fields, leg.legacy_injection, leg.legacy_criteria) == (True,) * 5
+    assert (leg.dt, leg.t_max, leg.r_inject_mm) == (1e-7, 1.0, 0.0)
+    monkeypatch.delenv("CHSIM_DT_DIV", raising=False)
+    cor = mq.Physics.correct(0.1)
+    assert (cor.dt, cor.t_max, cor.r_inject_mm) == (4e-8, 0.02, 2.0)
+    monkeypatch.setenv("CHSIM_DT_DIV", "100")
+    assert mq.Physics.correct(0.1).dt == 2e-8
+
+
+def _declared_functions():
+    names = []
+    for h in (ROOT / "include").glob("*.h"):
+        txt = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        names += re.findall(r"\b(mq_[a-z0-9_]+)\s*\(", txt)
+    return sorted(set(names))
+
+
+def test_library_exports_every_declared_symbol(built):
+    from multiq_workbench_gb300 import _native as N
+    L = N.lib()
+    names = _declared_functions()
+    assert len(names) >= 20
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_abi_refusals_without_device(coarse):
+    """Engine creation reports a status code (never aborts); with no device it is MQ_ERR_NO_DEVICE."""
+    import multiq_workbench_gb300 as mq
+    from multiq_workbench_gb300 import _native as N
+    L = N.lib()
+    h = C.c_void_p()
+    desc = coarse.grid_desc()
+    assert L.mq_engine_create(None, 0, 0, C.byref(h)) == -1
+    assert L.mq_engine_create(C.byref(desc), 7, 0, C.byref(h)) == -1
+    if mq.device_count() == 0:
+        assert L.mq_engine_create(C.byref(desc), 1, 0, C.byref(h)) == -6
+        with pytest.raises(mq.MqError):
+            mq.Engine(coarse)
+    # injection with a bad total and an RF mismatch is refused
+    ph = mq.Physics(pressure_pa=0.1)
+    jobs = [mq.Job(mq.Species(499.0, 1.0, 185.6), mq.RfAc(100.0, 500e3, 0.5, 1e5), 4, 1),
+            mq.Job(mq.Species(499.0, 1.0, 185.6), mq.RfAc(90.0, 500e3, 0.5, 1e5), 4, 2)]
+    with pytest.raises(mq.MqError) as ei:
+        mq.inject(coarse, jobs, ph)
+    assert ei.value.code == -5
+
+
+def test_summarize_c_matches_oracle(built):
+    import multiq_workbench_gb300 as mq
+    from oracle import mqref as R
+    rng = np.random.default_rng(5)
+    n = 1000
+    ions = mq.IonStates.empty(n)
+    ions.status[:] = rng.integers(0, 6, n)
+    ions.jid[:] = rng.integers(0, 7, n)
+    ions.ncoll[:] = rng.integers(0, 100, n)
+    ions.steps[:] = rng.integers(0, 20000, n)
+    a = mq.summarize(ions, 7, 1e-7)
+    s = R.State.from_arrays(ions)
+    b = R.Batch()
+    b.dt = 1e-7
+    o = R.summarize(s, b, 7)
+    for x, y in zip(a, o):
+        assert (x.n, x.crashed, x.returned, x.transmitted, x.left, x.timeout) == \
+               (y["n"], y["crashed"], y["returned"], y["transmitted"], y["left"], y["timeout"])
+        assert x.mean_coll == y["mean_coll"] and x.mean_time == y["mean_time"]
