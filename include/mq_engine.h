@@ -121,6 +121,7 @@ typedef struct mq_tuning {
     int32_t blocks_per_sm;       /* resident blocks per SM of the persistent grid (1..3)   */
     uint32_t chunk;              /* steps per ion per launch (compaction interval)         */
     int32_t use_graph;           /* replay the launch sequence as one CUDA graph           */
+    int32_t prefetch;            /* L1-prefetch the cell each ion is heading for           */
 } mq_tuning;
 mq_status   mq_engine_get_tuning(mq_engine* e, mq_tuning* t);
 mq_status   mq_engine_set_tuning(mq_engine* e, const mq_tuning* t);

@@ -2,9 +2,9 @@
 filiprumenovski/multiq-workbench).  Public API mirrors chsim: ``Geom``, ``Fields``,
 ``Species``, ``RfAc``, ``Job``, ``Physics``, ``Outcome``, ``Engine.run_batch``."""
 from .grid import Geom, Fields, cache_dir, cache_path
-from .channel import (Engine, Species, RfAc, Job, Physics, Outcome, IonStates, RunStats, MqError, summarize, inject,
+from .channel import (Engine, Species, RfAc, Job, JobTable, Physics, Outcome, IonStates, RunStats, MqError, summarize, inject,
                       device_count, PREC_F64, PREC_MIXED, LAUNCH_DISC, LAUNCH_LEGACY, LAUNCH_GAUSSIAN, STATUS)
 
-__all__ = ["Geom", "Fields", "cache_dir", "cache_path", "Engine", "Species", "RfAc", "Job", "Physics", "Outcome",
+__all__ = ["Geom", "Fields", "cache_dir", "cache_path", "Engine", "Species", "RfAc", "Job", "JobTable", "Physics", "Outcome",
            "IonStates", "RunStats", "MqError", "summarize", "inject", "device_count", "PREC_F64", "PREC_MIXED", "LAUNCH_DISC",
            "LAUNCH_LEGACY", "LAUNCH_GAUSSIAN", "STATUS"]

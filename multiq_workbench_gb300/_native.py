@@ -95,7 +95,7 @@ class mq_run_stats(C.Structure):
 
 class mq_tuning(C.Structure):
     _fields_ = [("threads_per_block", C.c_int32), ("blocks_per_sm", C.c_int32), ("chunk", C.c_uint32),
-                ("use_graph", C.c_int32)]
+                ("use_graph", C.c_int32), ("prefetch", C.c_int32)]
 
 
 def lib():

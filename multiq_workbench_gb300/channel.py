@@ -174,13 +174,58 @@ class IonStates:
         return np.stack([self.vx, self.vy, self.vz], 1)
 
 
-def jobs_native(jobs) -> C.Array:
-    arr = (N.mq_job * len(jobs))()
-    for k, j in enumerate(jobs):
-        arr[k].sp.mass, arr[k].sp.z, arr[k].sp.ccs_n2 = j.sp.mass, j.sp.z, j.sp.ccs_n2
-        arr[k].drive.v_rf, arr[k].drive.f_rf, arr[k].drive.v_ac, arr[k].drive.f_ac = j.drive.v_rf, j.drive.f_rf, j.drive.v_ac, j.drive.f_ac
-        arr[k].n, arr[k].seed = int(j.n), int(j.seed) & 0xFFFFFFFFFFFFFFFF
-    return arr
+JOB_DTYPE = np.dtype([("mass", "<f8"), ("z", "<f8"), ("ccs_n2", "<f8"), ("v_rf", "<f8"), ("f_rf", "<f8"),
+                      ("v_ac", "<f8"), ("f_ac", "<f8"), ("n", "<u8"), ("seed", "<u8")])
+assert JOB_DTYPE.itemsize == C.sizeof(N.mq_job)
+
+
+class JobTable:
+    """A batch of jobs packed once into the ABI's ``mq_job`` layout (optionally in pinned host
+    memory), so repeated calls pass a pointer instead of re-packing Python objects."""
+
+    def __init__(self, arr: np.ndarray, keep=None):
+        self.arr = arr
+        self._keep = keep
+
+    @classmethod
+    def from_jobs(cls, jobs, pinned: bool = False) -> "JobTable":
+        n = len(jobs)
+        keep = None
+        if pinned:
+            import torch   # page-locked host memory for the per-call host-to-device copy
+            keep = torch.empty(n * JOB_DTYPE.itemsize, dtype=torch.uint8, pin_memory=True)
+            arr = np.frombuffer(keep.numpy(), dtype=JOB_DTYPE, count=n)
+        else:
+            arr = np.empty(n, JOB_DTYPE)
+        arr[:] = [(j.sp.mass, j.sp.z, j.sp.ccs_n2, j.drive.v_rf, j.drive.f_rf, j.drive.v_ac, j.drive.f_ac, int(j.n),
+                   int(j.seed) & 0xFFFFFFFFFFFFFFFF) for j in jobs]
+        return cls(arr, keep)
+
+    def __len__(self) -> int:
+        return len(self.arr)
+
+    def total_ions(self) -> int:
+        return int(self.arr["n"].sum())
+
+    def ptr(self):
+        # data_as keeps a reference to the array, so a temporary table outlives the C call
+        return self.arr.ctypes.data_as(C.POINTER(N.mq_job))
+
+    def first(self):
+        a = self.arr[0]
+        return Job(Species(float(a["mass"]), float(a["z"]), float(a["ccs_n2"])),
+                   RfAc(float(a["v_rf"]), float(a["f_rf"]), float(a["v_ac"]), float(a["f_ac"])), int(a["n"]), int(a["seed"]))
+
+
+def jobs_native(jobs):
+    """ABI pointer to a job array (packs a list; passes a JobTable through)."""
+    if isinstance(jobs, JobTable):
+        return jobs.ptr()
+    return JobTable.from_jobs(jobs).ptr()
+
+
+def _total(jobs) -> int:
+    return jobs.total_ions() if isinstance(jobs, JobTable) else sum(int(j.n) for j in jobs)
 
 
 @dataclass
@@ -237,13 +282,15 @@ class Engine:
         t = N.mq_tuning()
         N.check(N.lib().mq_engine_get_tuning(self._h, C.byref(t)), "mq_engine_get_tuning", self._h)
         return dict(threads_per_block=t.threads_per_block, blocks_per_sm=t.blocks_per_sm, chunk=t.chunk,
-                    use_graph=bool(t.use_graph))
+                    use_graph=bool(t.use_graph), prefetch=bool(t.prefetch))
 
-    def set_tuning(self, blocks_per_sm: int | None = None, chunk: int | None = None, use_graph: bool | None = None) -> None:
+    def set_tuning(self, blocks_per_sm: int | None = None, chunk: int | None = None, use_graph: bool | None = None,
+                   prefetch: bool | None = None) -> None:
         cur = self.tuning()
         t = N.mq_tuning(128, int(blocks_per_sm if blocks_per_sm is not None else cur["blocks_per_sm"]),
                         int(chunk if chunk is not None else cur["chunk"]),
-                        int(use_graph if use_graph is not None else cur["use_graph"]))
+                        int(use_graph if use_graph is not None else cur["use_graph"]),
+                        int(prefetch if prefetch is not None else cur["prefetch"]))
         N.check(N.lib().mq_engine_set_tuning(self._h, C.byref(t)), "mq_engine_set_tuning", self._h)
 
     def autotune(self, jobs, dc, ph: Physics, sample_per_job: int = 2048) -> tuple[dict, float]:
@@ -261,7 +308,7 @@ class Engine:
 
     def inject(self, jobs, ph: Physics, pinned: bool = False) -> IonStates:
         """Initial states of every job's ions in job order (chsim ``Engine::inject``)."""
-        n = sum(int(j.n) for j in jobs)
+        n = _total(jobs)
         ions = IonStates.empty(n, pinned)
         io = ions.native()
         js = jobs_native(jobs)
@@ -291,7 +338,7 @@ class Engine:
 
     def run_batch_ions(self, jobs, dc, ph: Physics) -> tuple[IonStates, np.ndarray]:
         """Final per-ion states and the job id of each ion (channel.rs:458-475)."""
-        n = sum(int(j.n) for j in jobs)
+        n = _total(jobs)
         ions = IonStates.empty(n)
         self.run_batch(jobs, dc, ph, ions_out=ions)
         return ions, ions.jid.copy()
@@ -299,7 +346,7 @@ class Engine:
 
 def inject(fields: Fields, jobs, ph: Physics, pinned: bool = False) -> IonStates:
     """Host injection for a grid without an engine (no device needed)."""
-    n = sum(int(j.n) for j in jobs)
+    n = _total(jobs)
     ions = IonStates.empty(n, pinned)
     io = ions.native()
     desc = fields.grid_desc()

@@ -33,6 +33,22 @@ struct DevBuf {
     template <class T> T* as() const { return static_cast<T*>(p); }
 };
 
+// page-locked host staging area for the per-call job tables and counters (so the
+// host<->device copies of a call are true asynchronous DMA); grown only between calls
+struct HostBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+    cudaError_t grow(size_t bytes) {
+        if (bytes <= cap) return cudaSuccess;
+        if (p) { cudaFreeHost(p); p = nullptr; cap = 0; }
+        cudaError_t e = cudaMallocHost(&p, bytes);
+        if (e == cudaSuccess) cap = bytes;
+        return e;
+    }
+    void release() { if (p) cudaFreeHost(p); p = nullptr; cap = 0; }
+    char* at(size_t off) const { return static_cast<char*>(p) + off; }
+};
+
 constexpr uint32_t kTabCap = 1u << 20;        // phase-table length cap (longer runs evaluate directly)
 constexpr uint32_t kF64Chunk = 50000;         // steps per FP64 launch
 
@@ -54,6 +70,7 @@ struct mq_engine {
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     DevBuf ions[14];
     DevBuf jobc, jfirst, jseed, tabs, counters, misc;
+    HostBuf stage;                 // pinned staging: [job constants | job offsets | job seeds | counters]
     mqmix::Scratch mix;            // mixed-engine scratch (lists, queue counters, job table)
     mqmix::Tuning tune;            // launch shape of the mixed engine
 };
@@ -201,10 +218,26 @@ mq_status copy_ions(mq_engine* e, const mq_ions* io, size_t n, bool to_device, u
     return MQ_OK;
 }
 
-// job constants + phase tables on the device; returns table length
+// layout of the pinned staging area for a call with njobs jobs
+struct StageLayout {
+    size_t jc, first, seed, cnt, total;
+    explicit StageLayout(size_t njobs) {
+        auto up = [](size_t v) { return (v + 255) & ~size_t(255); };
+        jc = 0;
+        first = up(sizeof(JobC) * njobs);
+        seed = first + up(8 * (njobs + 1));
+        cnt = seed + up(8 * njobs);
+        total = cnt + up(sizeof(unsigned long long) * mqd::kCounters * njobs);
+    }
+};
+
+// job constants (and, for device injection, job offsets and seeds) staged in pinned memory
+// and uploaded; phase tables for the FP64 kernel; returns the table length
 mq_status upload_jobs(mq_engine* e, const mq_job* jobs, size_t njobs, const mq_physics& ph, const Batch& b,
-                      uint32_t* tlen_out, size_t* ntab_out) {
-    std::vector<JobC> jc(njobs);
+                      bool offsets, uint32_t* tlen_out, size_t* ntab_out, uint64_t* h2d) {
+    const StageLayout L(njobs);
+    CK(e->stage.grow(L.total), "pinned staging");
+    JobC* jc = reinterpret_cast<JobC*>(e->stage.at(L.jc));
     std::vector<double> tones;
     for (size_t k = 0; k < njobs; ++k) {
         jc[k] = make_job(jobs[k], ph);
@@ -216,7 +249,24 @@ mq_status upload_jobs(mq_engine* e, const mq_job* jobs, size_t njobs, const mq_p
     uint32_t tlen = b.max_steps < kTabCap ? b.max_steps : kTabCap;
     if (tlen == 0) tlen = 1;
     CK(e->jobc.grow(sizeof(JobC) * njobs), "job table");
-    CK(cudaMemcpyAsync(e->jobc.p, jc.data(), sizeof(JobC) * njobs, cudaMemcpyHostToDevice, e->st), "job table upload");
+    CK(cudaMemcpyAsync(e->jobc.p, jc, sizeof(JobC) * njobs, cudaMemcpyHostToDevice, e->st), "job table upload");
+    *h2d += sizeof(JobC) * njobs;
+    if (offsets) {
+        uint64_t* first = reinterpret_cast<uint64_t*>(e->stage.at(L.first));
+        uint64_t* seed = reinterpret_cast<uint64_t*>(e->stage.at(L.seed));
+        first[0] = 0;
+        for (size_t k = 0; k < njobs; ++k) { first[k + 1] = first[k] + jobs[k].n; seed[k] = jobs[k].seed; }
+        CK(e->jfirst.grow(8 * (njobs + 1)), "job offsets");
+        CK(e->jseed.grow(8 * njobs), "job seeds");
+        CK(cudaMemcpyAsync(e->jfirst.p, first, 8 * (njobs + 1), cudaMemcpyHostToDevice, e->st), "job upload");
+        CK(cudaMemcpyAsync(e->jseed.p, seed, 8 * njobs, cudaMemcpyHostToDevice, e->st), "job upload");
+        *h2d += 8 * (2 * njobs + 1);
+    }
+    if (e->prec == MQ_PREC_MIXED) {   // the mixed engine advances its phases itself: no tables
+        *tlen_out = 0;
+        *ntab_out = 0;
+        return MQ_OK;
+    }
     size_t ntab = 1 + tones.size();
     CK(e->tabs.grow(sizeof(double2) * (size_t)tlen * ntab), "phase tables");
     double2* t0 = e->tabs.as<double2>();
@@ -347,6 +397,7 @@ void mq_engine_destroy(mq_engine* e) {
     for (float4* p : {e->d_rf, e->d_ac, e->d_dc, e->d_dcb[0], e->d_dcb[1], e->d_dcb[2], e->d_dcb[3]}) if (p) cudaFree(p);
     for (auto& b : e->ions) b.release();
     e->jobc.release(); e->jfirst.release(); e->jseed.release(); e->tabs.release(); e->counters.release(); e->misc.release();
+    e->stage.release();
     mqmix::release(e->mix);
     for (auto& v : e->ev) if (v) cudaEventDestroy(v);
     if (e->st) cudaStreamDestroy(e->st);
@@ -422,7 +473,7 @@ mq_status mq_run_ions(mq_engine* e, const mq_job* jobs, size_t njobs, const mq_p
     if ((s = copy_ions(e, io, n, true, &h2d)) != MQ_OK) return s;
     uint32_t tlen = 0;
     size_t ntab = 0;
-    if ((s = upload_jobs(e, jobs, njobs, *ph, b, &tlen, &ntab)) != MQ_OK) return s;
+    if ((s = upload_jobs(e, jobs, njobs, *ph, b, false, &tlen, &ntab, &h2d)) != MQ_OK) return s;
     uint64_t steps = 0;
     if (e->prec == MQ_PREC_F64) s = run_f64(e, b, tlen, n, max_more, stats, &steps);
     else s = run_mixed(e, jobs, njobs, *ph, b, n, max_more, stats, &steps);
@@ -456,17 +507,10 @@ mq_status mq_run_batch(mq_engine* e, const mq_job* jobs, size_t njobs, const dou
     Batch b = make_batch(e, *ph, jobs[0].drive);
     if ((s = grow_ions(e, n)) != MQ_OK) return s;
     uint64_t h2d = 0, d2h = 0;
-    std::vector<uint64_t> first(njobs + 1), seed(njobs);
-    for (size_t k = 0; k < njobs; ++k) { first[k + 1] = first[k] + jobs[k].n; seed[k] = jobs[k].seed; }
     CK(cudaEventRecord(e->ev[0], e->st), "event");
     uint32_t tlen = 0;
     size_t ntab = 0;
-    if ((s = upload_jobs(e, jobs, njobs, *ph, b, &tlen, &ntab)) != MQ_OK) return s;
-    CK(e->jfirst.grow(8 * (njobs + 1)), "job offsets");
-    CK(e->jseed.grow(8 * njobs), "job seeds");
-    CK(cudaMemcpyAsync(e->jfirst.p, first.data(), 8 * (njobs + 1), cudaMemcpyHostToDevice, e->st), "job upload");
-    CK(cudaMemcpyAsync(e->jseed.p, seed.data(), 8 * njobs, cudaMemcpyHostToDevice, e->st), "job upload");
-    h2d += sizeof(JobC) * njobs + 8 * (2 * njobs + 1);
+    if ((s = upload_jobs(e, jobs, njobs, *ph, b, true, &tlen, &ntab, &h2d)) != MQ_OK) return s;
     mqd::JobTable jt;
     jt.jc = e->jobc.as<JobC>(); jt.first = e->jfirst.as<uint64_t>(); jt.seed = e->jseed.as<uint64_t>(); jt.njobs = (uint32_t)njobs;
     CK(mqd::launch_inject(b, jt, dev_ions(e), (uint32_t)n, e->st), "inject kernel");
@@ -477,9 +521,10 @@ mq_status mq_run_batch(mq_engine* e, const mq_job* jobs, size_t njobs, const dou
     CK(e->counters.grow(sizeof(unsigned long long) * mqd::kCounters * njobs), "job counters");
     CK(cudaMemsetAsync(e->counters.p, 0, sizeof(unsigned long long) * mqd::kCounters * njobs, e->st), "counter reset");
     CK(mqd::launch_summarize(dev_ions(e), (uint32_t)n, (uint32_t)njobs, e->counters.as<unsigned long long>(), e->st), "summary kernel");
-    std::vector<unsigned long long> cnt(mqd::kCounters * njobs);
-    CK(cudaMemcpyAsync(cnt.data(), e->counters.p, cnt.size() * 8, cudaMemcpyDeviceToHost, e->st), "counter download");
-    d2h += cnt.size() * 8;
+    const unsigned long long* cnt = reinterpret_cast<const unsigned long long*>(e->stage.at(StageLayout(njobs).cnt));
+    CK(cudaMemcpyAsync(e->stage.at(StageLayout(njobs).cnt), e->counters.p, sizeof(unsigned long long) * mqd::kCounters * njobs,
+                       cudaMemcpyDeviceToHost, e->st), "counter download");
+    d2h += sizeof(unsigned long long) * mqd::kCounters * njobs;
     if (ions_out && (s = copy_ions(e, ions_out, n, false, &d2h)) != MQ_OK) return s;
     CK(cudaEventRecord(e->ev[1], e->st), "event");
     CK(cudaStreamSynchronize(e->st), "run_batch");
@@ -508,6 +553,7 @@ mq_status mq_engine_get_tuning(mq_engine* e, mq_tuning* t) {
     t->blocks_per_sm = e->tune.blocks_per_sm;
     t->chunk = e->tune.chunk;
     t->use_graph = e->tune.use_graph;
+    t->prefetch = e->tune.prefetch;
     return MQ_OK;
 }
 
@@ -519,6 +565,7 @@ mq_status mq_engine_set_tuning(mq_engine* e, const mq_tuning* t) {
     e->tune.blocks_per_sm = t->blocks_per_sm;
     e->tune.chunk = t->chunk;
     e->tune.use_graph = t->use_graph ? 1 : 0;
+    e->tune.prefetch = t->prefetch ? 1 : 0;
     return MQ_OK;
 }
 
@@ -535,12 +582,14 @@ mq_status mq_engine_autotune(mq_engine* e, const mq_job* jobs, size_t njobs, con
     mqmix::Tuning top = keep;
     double top_rate = -1.0;
     const int blocks[] = {2, 3};
-    const uint32_t chunks[] = {1024, 2048, 4096, 8192, 20000};
+    const uint32_t chunks[] = {2048, 8192, 20000};
+    for (int pf = 0; pf < 2; ++pf)
     for (int bl : blocks)
         for (uint32_t ch : chunks) {
             e->tune = keep;
             e->tune.blocks_per_sm = bl;
             e->tune.chunk = ch;
+            e->tune.prefetch = pf;
             mq_run_stats st;
             // first call warms the graph and caches; the second is timed
             if ((s = mq_run_batch(e, sj.data(), njobs, dc, ph, out.data(), nullptr, &st)) != MQ_OK) { e->tune = keep; return s; }

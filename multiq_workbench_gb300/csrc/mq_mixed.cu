@@ -51,7 +51,8 @@ __device__ __forceinline__ uint4 philox(uint32_t k0, uint32_t k1, uint32_t c0, u
     }
     return make_uint4(c0, c1, c2, c3);
 }
-__device__ __forceinline__ float unif(uint32_t x) { return (float)(x >> 8) * 0x1.0p-24f; }
+__device__ __forceinline__ float unif(uint32_t x) { return (float)(x >> 8) * 0x1.0p-24f; }   // top 24 bits
+__device__ __forceinline__ float unif16(uint32_t x16) { return (float)x16 * 0x1.0p-16f; }      // a 16-bit field
 
 // ---------------------------------------------------------------- FP32 turn-based sine
 // sin / cos Taylor polynomials on [-pi/4, pi/4] (coefficients (-1)^k/(2k+1)!, (-1)^k/(2k)!)
@@ -69,14 +70,21 @@ __device__ __forceinline__ float cosp(float x) {
     p = fmaf(z, p, 0x1.555556p-5f);
     return fmaf(z * z, p, fmaf(z, -0.5f, 1.0f));
 }
-// sin(2 pi P / 2^64) for a 64-bit fixed-point phase in turns
-__device__ __forceinline__ float turn_sin(uint64_t P) {
+// sin and cos of 2 pi P / 2^64 for a 64-bit fixed-point phase in turns
+__device__ __forceinline__ void turn_sincos(uint64_t P, float& so, float& co) {
     int64_t r = (int64_t)(P << 2);                      // remainder of 4*phase in [-1/2, 1/2) quarter turns
     uint32_t q = (uint32_t)(P >> 62) + (r < 0 ? 1u : 0u);
     float x = (float)(int32_t)(r >> 32) * 0x1.921fb6p-32f;   // (pi/2) * 2^-32
     float s = sinp(x), c = cosp(x);
-    float v = (q & 1u) ? c : s;
-    return (q & 2u) ? -v : v;
+    float vs = (q & 1u) ? c : s, vc = (q & 1u) ? -s : c;
+    so = (q & 2u) ? -vs : vs;
+    co = (q & 2u) ? -vc : vc;
+}
+// one step of the drive: rotate (s, c) by the per-step angle (cw, sw)
+__device__ __forceinline__ void rotate(float& s, float& c, float cw, float sw) {
+    const float s2 = fmaf(s, cw, c * sw);
+    c = fmaf(c, cw, -(s * sw));
+    s = s2;
 }
 
 // ---------------------------------------------------------------- double-float helpers
@@ -89,8 +97,6 @@ __device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& 
     s = __fadd_rn(a, b);
     e = __fsub_rn(b, __fsub_rn(s, a));
 }
-__device__ __forceinline__ bool df_gt(float h, float l, float th, float tl) { return h > th || (h == th && l > tl); }
-__device__ __forceinline__ bool df_lt(float h, float l, float th, float tl) { return h < th || (h == th && l < tl); }
 
 // ---------------------------------------------------------------- cell cache
 // Interleaved node records: node q occupies float4 [3q] = {RF.xyz, conductor mask},
@@ -150,10 +156,13 @@ __device__ __forceinline__ float field_comp(const float R[8], const float D[8], 
 __device__ __forceinline__ int32_t clampi(int32_t v, int32_t lo, int32_t hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
 // ---------------------------------------------------------------- the persistent worker
-template <bool LEGACY>
+template <bool LEGACY, bool PREFETCH>
 __global__ void __launch_bounds__(128, 3)
 k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__ jobs, DevIons io,
-        const uint32_t* __restrict__ list_in, uint32_t* __restrict__ list_out, Ctrs* ctr, int in_slot, uint32_t chunk) {
+        const uint32_t* __restrict__ list_in, uint32_t* __restrict__ list_out, Ctrs* ctr, int in_slot, uint32_t chunk,
+        float* __restrict__ keep, uint32_t n_all, int resume) {
+    // keep: exact double-float position/velocity of ions re-queued by an earlier launch of the
+    // same call (12 floats per ion, structure of arrays over n_all); resume != 0 reads it
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t count = ctr->count[in_slot];
     if (count == 0) return;
@@ -165,6 +174,9 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
     float xh[3], xl[3], uh[3], ul[3];
     uint64_t Prf = 0, Pac = 0, Wac = 0;
     const uint64_t Wrf = ((uint64_t)B.w_rf_hi << 32) | B.w_rf_lo;
+    // drive sines advanced by rotation each step and re-evaluated exactly from the
+    // fixed-point phases every 16 loop iterations (warp-uniform), so rounding cannot build up
+    float srf = 0.f, crf = 1.f, sac = 0.f, cac = 1.f, cw_ac = 1.f, sw_ac = 0.f;
     float kick = 0.f, v_ac = 0.f, cand_a = 0.f, cand_b = 0.f;
     uint32_t k0 = 0, k1 = 0;
     // per-step candidate uniforms: Philox block n>>2 (rc) and the next block (rn); rn is
@@ -194,19 +206,36 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
                     const MixJob J = jobs[jid];
                     kick = J.kick; v_ac = J.use_ac ? J.v_ac : 0.0f; cand_a = J.cand_a; cand_b = J.cand_b;
                     Wac = ((uint64_t)J.w_ac_hi << 32) | J.w_ac_lo;
+                    cw_ac = J.cw_ac; sw_ac = J.sw_ac;
                     n = io.steps[id]; ncoll = io.ncoll[id]; leg = io.leg[id];
-                    const double gx[3] = {io.x[id] * B.inv_h, io.y[id] * B.inv_h, io.z[id] * B.inv_h};
-                    const double gu[3] = {io.vx[id] * B.v2u, io.vy[id] * B.v2u, io.vz[id] * B.v2u};
+                    if (resume) {
 #pragma unroll
-                    for (int d = 0; d < 3; ++d) {
-                        xh[d] = (float)gx[d]; xl[d] = (float)(gx[d] - (double)xh[d]);
-                        uh[d] = (float)gu[d]; ul[d] = (float)(gu[d] - (double)uh[d]);
+                        for (int d = 0; d < 3; ++d) {
+                            xh[d] = keep[(size_t)(0 + d) * n_all + id]; xl[d] = keep[(size_t)(3 + d) * n_all + id];
+                            uh[d] = keep[(size_t)(6 + d) * n_all + id]; ul[d] = keep[(size_t)(9 + d) * n_all + id];
+                        }
+                    } else {
+                        const double gx[3] = {io.x[id] * B.inv_h, io.y[id] * B.inv_h, io.z[id] * B.inv_h};
+                        const double gu[3] = {io.vx[id] * B.v2u, io.vy[id] * B.v2u, io.vz[id] * B.v2u};
+#pragma unroll
+                        for (int d = 0; d < 3; ++d) {
+                            xh[d] = (float)gx[d]; xl[d] = (float)(gx[d] - (double)xh[d]);
+                            uh[d] = (float)gu[d]; ul[d] = (float)(gu[d] - (double)uh[d]);
+                        }
                     }
                     // phase = offset + n * w (mod 1) in 64-bit fixed point
                     const double prf = io.ph_rf[id], pac = io.ph_ac[id];
                     const uint64_t orf = (uint64_t)(prf * 0x1.0p63) << 1, oac = (uint64_t)(pac * 0x1.0p63) << 1;
                     Prf = orf + (uint64_t)n * Wrf;
                     Pac = oac + (uint64_t)n * Wac;
+                    // drive state as an uninterrupted run has it: exact at the last step that is
+                    // a multiple of 16, then rotated forward (so re-queued ions continue bitwise)
+                    {
+                        const uint32_t r16 = n & 15u;
+                        turn_sincos(Prf - (uint64_t)r16 * Wrf, srf, crf);
+                        turn_sincos(Pac - (uint64_t)r16 * Wac, sac, cac);
+                        for (uint32_t q = 0; q < r16; ++q) { rotate(srf, crf, B.cw_rf, B.sw_rf); rotate(sac, cac, cw_ac, sw_ac); }
+                    }
                     const uint64_t key = io.rng[id];
                     k0 = (uint32_t)key; k1 = (uint32_t)(key >> 32);
                     if (!LEGACY) { rc = philox(k0, k1, n >> 2, 0u, 0u, 0u); rn = philox(k0, k1, (n >> 2) + 1u, 0u, 0u, 0u); }
@@ -222,9 +251,16 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
         if (!__any_sync(FULL, have)) break;
 
         bool append = false;
-        if (!LEGACY && (iter & 3u) == 0u && have) rn = philox(k0, k1, (n >> 2) + 1u, 0u, 0u, 0u);
+        // A lane steps its ion only when the ion's step count is congruent to the warp's
+        // iteration counter mod 16 (a freshly loaded ion waits at most 15 iterations).  Every
+        // warp-uniform event below (Philox refresh each 4 iterations, exact drive re-sync
+        // each 16) then falls on the same steps of every ion, whatever the scheduling, so
+        // per-ion results are reproducible bit for bit.
+        const bool act = have && (((iter ^ n) & 15u) == 0u);
+        if (!LEGACY && (iter & 3u) == 0u && act) rn = philox(k0, k1, (n >> 2) + 1u, 0u, 0u, 0u);
+        if ((iter & 15u) == 0u && act) { turn_sincos(Prf, srf, crf); turn_sincos(Pac, sac, cac); }
         ++iter;
-        if (have) {
+        if (act) {
             // ---- field at the current position
             float tx = 0.f, ty = 0.f, tz = 0.f;
             if (!B.nearest) {
@@ -232,8 +268,8 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
                 ty = __fadd_rn(__fsub_rn(xh[1], (float)c.cj), xl[1]);
                 tz = __fadd_rn(__fsub_rn(xh[2], (float)c.ck), xl[2]);
             }
-            const float a_rf = B.v_rf * turn_sin(Prf);
-            const float a_ac = v_ac * turn_sin(Pac);
+            const float a_rf = B.v_rf * srf;
+            const float a_ac = v_ac * sac;
             float E[3];
 #pragma unroll
             for (int d = 0; d < 3; ++d) E[d] = field_comp(c.R[d], c.D[d], c.A[d], a_rf, a_ac, tx, ty, tz);
@@ -249,6 +285,8 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
             }
             Prf += Wrf;
             Pac += Wac;
+            rotate(srf, crf, B.cw_rf, B.sw_rf);
+            rotate(sac, cac, cw_ac, sw_ac);
             const uint32_t nprev = n;
             n += 1;
             done += 1;
@@ -258,26 +296,27 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
                 const float um = sqrtf(fmaf(uh[0], uh[0], fmaf(uh[1], uh[1], uh[2] * uh[2])));
                 if (u0 < fmaf(cand_a, um, cand_b)) {
                     const MixJob J = jobs[jid];
-                    // gas velocity: three normals from four uniforms (two Box-Muller radii);
-                    // acceptance and the isotropic direction from a second block
-                    const uint4 r0 = philox(k0, k1, nprev, 1u, 0u, 0u), r1 = philox(k0, k1, nprev, 1u, 1u, 0u);
+                    // one Philox block (128 bits) per candidate: two 24-bit uniforms for the
+                    // Box-Muller radii, and five 16-bit uniforms (two Box-Muller angles, the
+                    // acceptance draw, cos(theta) and phi of the scattering direction)
+                    const uint4 r0 = philox(k0, k1, nprev, 1u, 0u, 0u);
                     const float u2v = B.u2v_f;
                     float v[3] = {uh[0] * u2v, uh[1] * u2v, uh[2] * u2v};
                     const float bound = fmaf(um, u2v, 6.0f * J.s_gas);
                     const float g1 = sqrtf(-2.0f * logf(fmaxf(unif(r0.x), 0x1.0p-25f)));
-                    const float g2 = sqrtf(-2.0f * logf(fmaxf(unif(r0.z), 0x1.0p-25f)));
+                    const float g2 = sqrtf(-2.0f * logf(fmaxf(unif(r0.y), 0x1.0p-25f)));
                     float s1, c1;
-                    sincospif(2.0f * unif(r0.y), &s1, &c1);
-                    const float c2 = cospif(2.0f * unif(r0.w));
+                    sincospif(2.0f * unif16(r0.z >> 16), &s1, &c1);
+                    const float c2 = cospif(2.0f * unif16(r0.z & 0xffffu));
                     float gv[3];
                     gv[0] = fmaf(-J.s_gas, g1 * c1, v[0]);
                     gv[1] = fmaf(-J.s_gas, g1 * s1, v[1]);
                     gv[2] = fmaf(-J.s_gas, g2 * c2, v[2]);
                     const float gl = sqrtf(fmaf(gv[0], gv[0], fmaf(gv[1], gv[1], gv[2] * gv[2])));
-                    if (unif(r1.x) * bound < gl) {
-                        const float cth = 2.0f * unif(r1.y) - 1.0f;
+                    if (unif16(r0.w >> 16) * bound < gl) {
+                        const float cth = 2.0f * unif16(r0.w & 0xffffu) - 1.0f;
                         float sp, cp;
-                        sincospif(2.0f * unif(r1.z), &sp, &cp);
+                        sincospif(2.0f * unif16(((r0.x & 0xffu) << 8) | (r0.y & 0xffu)), &sp, &cp);
                         const float sn = sqrtf(fmaxf(0.0f, 1.0f - cth * cth));
                         const float nn[3] = {sn * cp, sn * sp, cth};
                         const float v2u = B.v2u_f;
@@ -320,25 +359,25 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
             }
             // ---- cell of the new position (refresh the cache before the conductor test), and
             //      an L1 prefetch of the cell one more step ahead
-            const int32_t ci = clampi(__float2int_rd(xh[0]), 0, B.nx - 2);
-            const int32_t cj = clampi(__float2int_rd(xh[1]), 0, B.ny - 2);
-            const int32_t ck = clampi(__float2int_rd(xh[2]), 0, B.nz - 2);
+            const int32_t fi = __float2int_rd(xh[0]), fj = __float2int_rd(xh[1]), fk = __float2int_rd(xh[2]);
+            const int32_t ci = clampi(fi, 0, B.nx - 2), cj = clampi(fj, 0, B.ny - 2), ck = clampi(fk, 0, B.nz - 2);
             if (ci != c.ci || cj != c.cj || ck != c.ck) load_cell(nodes, B, ci, cj, ck, c);
-            {
+            if (PREFETCH) {
                 const int32_t pi = clampi(__float2int_rd(xh[0] + uh[0]), 0, B.nx - 2);
                 const int32_t pj = clampi(__float2int_rd(xh[1] + uh[1]), 0, B.ny - 2);
                 const int32_t pk = clampi(__float2int_rd(xh[2] + uh[2]), 0, B.nz - 2);
                 if (pi != ci || pj != cj || pk != ck) prefetch_cell(nodes, B, pi, pj, pk);
             }
             // ---- termination tests: exit, return, box, conductor, timeout
+            // (a position exactly on a threshold is resolved by the high part alone; the box
+            // test is the unclamped cell index leaving [0, n-2])
             int32_t status = 0;
-            if (df_gt(xh[2], xl[2], B.z_exit_h, B.z_exit_l)) status = 3;
-            else if (df_lt(xh[2], xl[2], B.z_ret_h, B.z_ret_l)) status = 2;
-            else if (df_lt(xh[0], xl[0], 0.f, 0.f) || df_lt(xh[1], xl[1], 0.f, 0.f) || df_lt(xh[2], xl[2], 0.f, 0.f) ||
-                     df_gt(xh[0], xl[0], B.lim_x, 0.f) || df_gt(xh[1], xl[1], B.lim_y, 0.f) || df_gt(xh[2], xl[2], B.lim_z, 0.f))
+            if (xh[2] > B.z_exit_h) status = 3;
+            else if (xh[2] < B.z_ret_h) status = 2;
+            else if ((uint32_t)fi > (uint32_t)(B.nx - 2) || (uint32_t)fj > (uint32_t)(B.ny - 2) || (uint32_t)fk > (uint32_t)(B.nz - 2))
                 status = 4;
             else {
-                if (df_gt(xh[2], xl[2], B.cz0_h, B.cz0_l) && df_lt(xh[2], xl[2], B.cz1_h, B.cz1_l)) {
+                if (xh[2] > B.cz0_h && xh[2] < B.cz1_h) {
                     const float fx = __fadd_rn(__fsub_rn(xh[0], (float)ci), xl[0]);
                     const float fy = __fadd_rn(__fsub_rn(xh[1], (float)cj), xl[1]);
                     const float fz = __fadd_rn(__fsub_rn(xh[2], (float)ck), xl[2]);
@@ -358,6 +397,13 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
                 io.steps[id] = n; io.ncoll[id] = ncoll; io.leg[id] = leg; io.status[id] = status;
                 steps_total += done;
                 append = status == 0;
+                if (append && keep) {
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) {
+                        keep[(size_t)(0 + d) * n_all + id] = xh[d]; keep[(size_t)(3 + d) * n_all + id] = xl[d];
+                        keep[(size_t)(6 + d) * n_all + id] = uh[d]; keep[(size_t)(9 + d) * n_all + id] = ul[d];
+                    }
+                }
                 have = false;
             }
         }
@@ -436,6 +482,10 @@ MixJob make_mix_job(const mqp::JobC& j, const mqp::Batch& b) {
     uint64_t w = fix64(j.w_ac);
     m.w_ac_lo = (uint32_t)w;
     m.w_ac_hi = (uint32_t)(w >> 32);
+    double s, c;
+    mqp::sincos2pi(j.w_ac, &s, &c);
+    m.cw_ac = (float)c;
+    m.sw_ac = (float)s;
     m.use_ac = j.use_ac;
     return m;
 }
@@ -455,6 +505,10 @@ MixBatch make_mix_batch(const mqp::Batch& b) {
     uint64_t w = fix64(b.w_rf);
     m.w_rf_lo = (uint32_t)w;
     m.w_rf_hi = (uint32_t)(w >> 32);
+    double s, c;
+    mqp::sincos2pi(b.w_rf, &s, &c);
+    m.cw_rf = (float)c;
+    m.sw_rf = (float)s;
     split(b.z_exit / b.h, m.z_exit_h, m.z_exit_l);
     split(b.z_return / b.h, m.z_ret_h, m.z_ret_l);
     split(b.crash_z0 / b.h, m.cz0_h, m.cz0_l);
@@ -479,7 +533,7 @@ Tuning default_tuning(int device) {
 
 void release(Scratch& s) {
     if (s.graph) cudaGraphExecDestroy(s.graph);
-    for (void* p : {s.lists, s.ctrs, s.params, s.jobs, s.nodes}) if (p) cudaFree(p);
+    for (void* p : {s.lists, s.ctrs, s.params, s.jobs, s.nodes, s.keep}) if (p) cudaFree(p);
     for (auto& e : s.ev) if (e) cudaEventDestroy(e);
     s = Scratch();
 }
@@ -491,15 +545,21 @@ static cudaError_t enqueue_launches(const Scratch& s, const Tuning& t, const Mix
     Ctrs* ctr = static_cast<Ctrs*>(s.ctrs);
     const MixJob* jobs = static_cast<const MixJob*>(s.jobs);
     const float4* nodes = static_cast<const float4*>(s.nodes);
+    float* keep = static_cast<float*>(s.keep);
     const int grid = t.sms * t.blocks_per_sm;
     for (uint32_t L = 0; L < launches; ++L) {
         const int in = (int)(L & 1);
         k_prep<<<1, 1, 0, st>>>(ctr, in ^ 1);
         const uint32_t ch = (L + 1 == launches) ? last_chunk : chunk;
-        if (mb.legacy_coll)
-            k_mixed<true><<<grid, t.tpb, 0, st>>>(nodes, mb, jobs, io, lists + (size_t)in * n, lists + (size_t)(in ^ 1) * n, ctr, in, ch);
-        else
-            k_mixed<false><<<grid, t.tpb, 0, st>>>(nodes, mb, jobs, io, lists + (size_t)in * n, lists + (size_t)(in ^ 1) * n, ctr, in, ch);
+        const uint32_t* li = lists + (size_t)in * n;
+        uint32_t* lo = lists + (size_t)(in ^ 1) * n;
+        if (mb.legacy_coll) {
+            if (t.prefetch) k_mixed<true, true><<<grid, t.tpb, 0, st>>>(nodes, mb, jobs, io, li, lo, ctr, in, ch, keep, n, L > 0);
+            else k_mixed<true, false><<<grid, t.tpb, 0, st>>>(nodes, mb, jobs, io, li, lo, ctr, in, ch, keep, n, L > 0);
+        } else {
+            if (t.prefetch) k_mixed<false, true><<<grid, t.tpb, 0, st>>>(nodes, mb, jobs, io, li, lo, ctr, in, ch, keep, n, L > 0);
+            else k_mixed<false, false><<<grid, t.tpb, 0, st>>>(nodes, mb, jobs, io, li, lo, ctr, in, ch, keep, n, L > 0);
+        }
         *kernels += 2;
     }
     return cudaGetLastError();
@@ -549,10 +609,18 @@ cudaError_t run(Scratch& s, const Tuning& t, DevGrid g, uint64_t grid_gen, const
     const MixBatch mb = make_mix_batch(b);
     // launches needed: every live ion has at most min(max_more, max_steps) steps left
     const uint64_t need = max_more < b.max_steps ? (uint64_t)max_more : (uint64_t)b.max_steps;
+    if (need == 0) return cudaSuccess;
     const uint32_t chunk = t.chunk ? t.chunk : 4096;
-    uint32_t launches = (uint32_t)((need + chunk - 1) / chunk);
-    if (launches == 0) launches = 1;
-    const uint32_t last_chunk = (uint32_t)(need - (uint64_t)(launches - 1) * chunk) ? (uint32_t)(need - (uint64_t)(launches - 1) * chunk) : chunk;
+    const uint32_t launches = (uint32_t)((need + chunk - 1) / chunk);
+    const uint32_t last_chunk = (uint32_t)(need - (uint64_t)(launches - 1) * chunk);
+    // exact double-float state of re-queued ions (only when the call spans several launches)
+    const size_t keep_bytes = launches > 1 ? (size_t)12 * n * sizeof(float) : 0;
+    if (s.keep_cap < keep_bytes) {
+        if (s.keep) cudaFree(s.keep);
+        s.keep = nullptr; s.keep_cap = 0;
+        if ((e = cudaMalloc(&s.keep, keep_bytes)) != cudaSuccess) return e;
+        s.keep_cap = keep_bytes;
+    }
     Ctrs* ctr = static_cast<Ctrs*>(s.ctrs);
     if ((e = cudaMemsetAsync(ctr, 0, sizeof(Ctrs), st)) != cudaSuccess) return e;
     k_init_list<<<(n + 255) / 256, 256, 0, st>>>(io, n, static_cast<uint32_t*>(s.lists), ctr);
@@ -563,7 +631,8 @@ cudaError_t run(Scratch& s, const Tuning& t, DevGrid g, uint64_t grid_gen, const
     const bool graph = t.use_graph && launches > 1;
     if (graph) {
         const uint64_t key[6] = {(uint64_t)(uintptr_t)s.lists, (uint64_t)n, launches, ((uint64_t)chunk << 32) | last_chunk,
-                                 (uint64_t)(uintptr_t)io.x ^ ((uint64_t)t.blocks_per_sm << 56), (uint64_t)(uintptr_t)s.nodes};
+                                 (uint64_t)(uintptr_t)io.x ^ ((uint64_t)t.blocks_per_sm << 56) ^ ((uint64_t)t.prefetch << 60),
+                                 (uint64_t)(uintptr_t)s.nodes ^ ((uint64_t)mb.legacy_coll << 62)};
         cudaGraph_t gr = nullptr;
         if ((e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return e;
         enqueue_launches(s, t, mb, io, n, launches, chunk, last_chunk, st, &kernels);

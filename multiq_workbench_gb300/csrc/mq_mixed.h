@@ -18,6 +18,7 @@ struct MixJob {
     float floor_v;     // legacy: no collision below this speed [m/s]; < 0 = thermal gas
     float mfp_mean;    // legacy mean free path [m]
     uint32_t w_ac_lo, w_ac_hi;   // AC phase increment per step, turns * 2^64
+    float cw_ac, sw_ac;          // cos / sin of the AC phase advance per step
     int32_t use_ac;
     int32_t pad;
 };
@@ -26,6 +27,7 @@ struct MixBatch {      // per-batch constants (device-resident parameter block)
     double h, inv_h, dt, u2v, v2u;   // u2v = h / dt (cells/step -> m/s)
     float v_rf, dt_f, u2v_f, v2u_f;
     uint32_t w_rf_lo, w_rf_hi;       // RF phase increment per step, turns * 2^64
+    float cw_rf, sw_rf;              // cos / sin of the RF phase advance per step
     float z_exit_h, z_exit_l, z_ret_h, z_ret_l;       // grid units, double-float
     float cz0_h, cz0_l, cz1_h, cz1_l;                 // crash window, grid units
     float lim_x, lim_y, lim_z;                        // n - 1 (exact)
@@ -37,9 +39,10 @@ struct MixBatch {      // per-batch constants (device-resident parameter block)
 
 struct Tuning {
     int tpb = 128;             // threads per block
-    int blocks_per_sm = 4;     // resident blocks per SM for the persistent grid
-    uint32_t chunk = 4096;     // steps per ion per launch (compaction interval)
+    int blocks_per_sm = 3;     // resident blocks per SM for the persistent grid (168 registers/thread)
+    uint32_t chunk = 20000;    // steps per ion per launch (compaction interval)
     int use_graph = 1;         // replay the launch sequence as one CUDA graph
+    int prefetch = 0;          // L1-prefetch the cell an ion is heading for
     int sms = 0;               // filled from the device
 };
 
@@ -50,6 +53,8 @@ struct Scratch {
     void* params = nullptr;    // MixBatch
     void* jobs = nullptr;      // MixJob[]
     size_t jobs_cap = 0;
+    void* keep = nullptr;      // exact double-float state of ions re-queued between launches
+    size_t keep_cap = 0;
     void* nodes = nullptr;     // interleaved RF | DC | AC node records (float4 x 3 per node)
     size_t nodes_cap = 0;
     uint64_t nodes_gen = ~0ull; // grid generation the records were packed from
