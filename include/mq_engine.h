@@ -131,6 +131,46 @@ mq_status   mq_engine_set_tuning(mq_engine* e, const mq_tuning* t);
 mq_status   mq_engine_autotune(mq_engine* e, const mq_job* jobs, size_t njobs, const double dc[4], const mq_physics* ph,
                                uint64_t sample_per_job, mq_tuning* best, double* best_rate);
 
+/* ---------------------------------------------------------------------------------------
+ * Allocation-free FP64 stepping (no counterpart in the reference).
+ *
+ * For callers that cannot allocate device memory themselves: code that runs inside a host
+ * framework or a plugin host that owns every device allocation (its own pool allocator,
+ * a captured or pre-planned memory budget), or that must not call cudaMalloc/cudaFree on
+ * the path because those calls synchronise the device.  Such a caller owns the field arrays
+ * and the ion states in device memory and passes pointers to them; this call advances the
+ * states exactly like mq_run_ions with MQ_PREC_F64 (same kernel, same results bit for bit)
+ * and allocates nothing: its working memory (the per-job constant table and two counters)
+ * is a fixed array in the library's static device memory, MQ_NOALLOC_SCRATCH_BYTES bytes,
+ * which every GPU that loads the library holds until the process exits.
+ *
+ * Limits and rules:
+ *  - njobs <= MQ_NOALLOC_MAX_JOBS; larger batches return MQ_ERR_TOO_LARGE (nothing is run).
+ *  - The first call on a device looks up the scratch array's device address (once per
+ *    device, with that device current); make that first call before any stream capture.
+ *  - All calls share the one scratch array (its contents persist between calls; the call
+ *    clears the counters it needs).  Calls that overlap on the GPU - from two host threads,
+ *    or on two streams - race on it and must be serialised by the caller.
+ *  - The drive phases are evaluated directly each step (the FP64 engine's phase tables are
+ *    the same values, precomputed), so no table memory is needed.
+ *  - Synchronous: returns after the last step, with *ion_steps (may be NULL) = executed steps.
+ */
+#define MQ_NOALLOC_MAX_JOBS 4096
+#define MQ_NOALLOC_SCRATCH_BYTES (MQ_NOALLOC_MAX_JOBS * 96 + 256)
+typedef struct mq_dev_grid {
+    int32_t nx, ny, nz, pad;
+    double h;                 /* spacing [m]                                        */
+    const float* rf4;         /* device: RF E per volt, w = conductor mask          */
+    const float* ac4;         /* device: AC E per volt                              */
+    const float* dc4;         /* device: combined static DC E (mq_dc_combine)        */
+    double axis_mm;
+    double layers_mm[8];
+} mq_dev_grid;
+/* dev_ions: every pointer of the mq_ions struct is a DEVICE pointer (n entries each). */
+mq_status   mq_run_ions_device_noalloc(const mq_dev_grid* grid, const mq_job* jobs, size_t njobs, const mq_physics* ph,
+                                       const mq_ions* dev_ions, size_t n, uint32_t max_more, void* stream,
+                                       uint64_t* ion_steps);
+
 #ifdef __cplusplus
 }
 #endif

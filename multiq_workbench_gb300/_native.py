@@ -93,6 +93,12 @@ class mq_run_stats(C.Structure):
                 ("step_kernel_ms", C.c_double), ("step_kernel_launches", C.c_uint32), ("pad", C.c_uint32)]
 
 
+class mq_dev_grid(C.Structure):
+    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32), ("pad", C.c_int32), ("h", C.c_double),
+                ("rf4", C.c_void_p), ("ac4", C.c_void_p), ("dc4", C.c_void_p), ("axis_mm", C.c_double),
+                ("layers_mm", C.c_double * 8)]
+
+
 class mq_tuning(C.Structure):
     _fields_ = [("threads_per_block", C.c_int32), ("blocks_per_sm", C.c_int32), ("chunk", C.c_uint32),
                 ("use_graph", C.c_int32), ("prefetch", C.c_int32)]
@@ -168,6 +174,9 @@ def _declare_engine(L) -> None:
     L.mq_engine_autotune.argtypes = [C.c_void_p, P(mq_job), C.c_size_t, P(C.c_double), P(mq_physics), C.c_uint64,
                                      P(mq_tuning), P(C.c_double)]
     L.mq_engine_autotune.restype = C.c_int32
+    L.mq_run_ions_device_noalloc.argtypes = [P(mq_dev_grid), P(mq_job), C.c_size_t, P(mq_physics), P(mq_ions), C.c_size_t,
+                                             C.c_uint32, C.c_void_p, P(C.c_uint64)]
+    L.mq_run_ions_device_noalloc.restype = C.c_int32
 
 
 def check(code: int, what: str, eng=None) -> None:

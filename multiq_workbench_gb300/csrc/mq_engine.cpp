@@ -350,6 +350,18 @@ mq_status run_mixed(mq_engine* e, const mq_job* jobs, size_t njobs, const mq_phy
 
 }  // namespace
 
+// batch and job constants for code outside this file (same functions the engine uses)
+namespace mqd {
+Batch host_batch(int32_t nx, int32_t ny, int32_t nz, double h, double axis_mm, const double layers_mm[8],
+                 const mq_physics& ph, const mq_rfac& rf) {
+    mq_engine tmp;   // geometry only
+    tmp.nx = nx; tmp.ny = ny; tmp.nz = nz; tmp.h = h; tmp.axis_mm = axis_mm;
+    for (int i = 0; i < 8; ++i) tmp.layers[i] = layers_mm[i];
+    return make_batch(&tmp, ph, rf);
+}
+JobC host_job(const mq_job& j, const mq_physics& ph) { return make_job(j, ph); }
+}  // namespace mqd
+
 extern "C" {
 
 int32_t mq_device_count(void) {

@@ -44,3 +44,14 @@ cudaError_t launch_dc_combine(const float4* b0, const float4* b1, const float4* 
 cudaError_t launch_summarize(DevIons io, uint32_t n, uint32_t njobs, unsigned long long* counters, cudaStream_t s);
 
 }  // namespace mqd
+
+struct mq_physics;
+struct mq_rfac;
+struct mq_job;
+namespace mqd {
+// ---- mq_engine.cpp: the engine's batch / job constants for other translation units
+mqp::Batch host_batch(int32_t nx, int32_t ny, int32_t nz, double h, double axis_mm, const double layers_mm[8],
+                      const mq_physics& ph, const mq_rfac& rf);
+mqp::JobC host_job(const mq_job& j, const mq_physics& ph);
+
+}  // namespace mqd
