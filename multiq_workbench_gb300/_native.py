@@ -1,4 +1,5 @@
-"""ctypes view of ``libmqgb.so`` (declarations in include/mq_grid.h and include/mq_engine.h).
+"""ctypes view of ``libmqgb.so`` (declarations in include/mq_grid.h, include/mq_engine.h and
+include/mq_tandem.h).
 
 The library is built in-tree by :mod:`multiq_workbench_gb300.build`.  Loading fails
 loudly if it is missing: there is no Python or CPU fallback for any engine call.
@@ -104,6 +105,47 @@ class mq_tuning(C.Structure):
                 ("use_graph", C.c_int32), ("prefetch", C.c_int32)]
 
 
+class mq_cube_geom(C.Structure):
+    _fields_ = [("n", C.c_int32), ("array", C.c_int32)] + [
+        (k, C.c_double) for k in ("d", "pitch", "height", "t_pcb", "gap", "stem_r", "clear_r", "l_ext", "ap_r",
+                                  "rod_clear_extra", "cap_gap", "cap_r")
+    ] + [("ent_axis", C.c_int32), ("ent_side", C.c_int32), ("ent_cell", C.c_int32 * 2),
+         ("ext_axis", C.c_int32), ("ext_side", C.c_int32), ("ext_cell", C.c_int32 * 2)]
+
+
+class mq_tandem_port(C.Structure):
+    _fields_ = [("dims", C.c_int32 * 3), ("pad", C.c_int32), ("h", C.c_double), ("rf4", C.c_void_p),
+                ("ac4", C.c_void_p), ("dc4", C.c_void_p), ("gate4", C.c_void_p), ("tone_khz", C.c_double),
+                ("v_ac", C.c_double)]
+
+
+class mq_tandem_species(C.Structure):
+    _fields_ = [("mass", C.c_double), ("z", C.c_double), ("ccs", C.c_double), ("weight", C.c_double)]
+
+
+class mq_tandem_desc(C.Structure):
+    _fields_ = [("cube", mq_cube_geom), ("cube_dims", C.c_int32 * 3), ("pad0", C.c_int32),
+                ("cube_lo_mm", C.c_double * 3), ("cube_h_mm", C.c_double), ("cube_rf4", C.c_void_p),
+                ("cube_dc4", C.c_void_p * 2), ("port", mq_tandem_port * 9), ("ch_axis_mm", C.c_double),
+                ("ch_q1_start_mm", C.c_double), ("v_rf", C.c_double), ("f_rf", C.c_double),
+                ("pressure_pa", C.c_double), ("temp_k", C.c_double), ("dt", C.c_double), ("gate_bias_v", C.c_double),
+                ("nspecies", C.c_int32), ("pad2", C.c_int32), ("species", mq_tandem_species * 8)]
+
+
+class mq_tracks(C.Structure):
+    _fields_ = [(k, C.c_void_p) for k in ("x", "y", "z", "vx", "vy", "vz", "rng", "sp", "region", "last")]
+
+
+class mq_port_counts(C.Structure):
+    _fields_ = [("entered", C.c_uint32), ("returned", C.c_uint32), ("forwarded", C.c_uint32),
+                ("revisits", C.c_uint32), ("from_other", C.c_uint32), ("retry_from", C.c_uint32 * 9),
+                ("reverse_entries", C.c_uint32), ("lost", C.c_uint32), ("by_charge", C.c_uint32 * 5)]
+
+
+class mq_tandem_frame_counts(C.Structure):
+    _fields_ = [(k, C.c_uint64) for k in ("split", "channel", "combine", "lost", "back", "detected")]
+
+
 def lib():
     """The loaded native library (raises if it has not been built)."""
     global _lib
@@ -141,6 +183,49 @@ def _declare(L) -> None:
     L.mq_dc_combine.restype = C.c_int32
     if hasattr(L, "mq_engine_create"):
         _declare_engine(L)
+    if hasattr(L, "mq_tandem_create"):
+        _declare_tandem(L)
+
+
+def _declare_tandem(L) -> None:
+    P = C.POINTER
+    L.mq_cube_as_built.argtypes = [P(mq_cube_geom)]
+    L.mq_cube_as_built.restype = None
+    L.mq_cube_snap.argtypes = [P(mq_cube_geom), C.c_double, P(mq_cube_geom), P(C.c_double)]
+    L.mq_cube_snap.restype = C.c_int32
+    L.mq_cube_classify.argtypes = [P(mq_cube_geom), P(C.c_double), C.c_double, P(C.c_int32)]
+    L.mq_cube_classify.restype = C.c_int32
+    L.mq_cube_size.argtypes = [P(mq_cube_geom)]
+    L.mq_cube_size.restype = C.c_double
+    L.mq_cube_post_top_depth.argtypes = [P(mq_cube_geom)]
+    L.mq_cube_post_top_depth.restype = C.c_double
+    L.mq_cube_nearest_port.argtypes = [P(mq_cube_geom), C.c_double, C.c_double]
+    L.mq_cube_nearest_port.restype = C.c_int32
+    L.mq_cube_port_axis.argtypes = [P(mq_cube_geom), C.c_int32, P(C.c_double)]
+    L.mq_cube_port_axis.restype = C.c_int32
+    L.mq_efield_fieldsolve.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_void_p]
+    L.mq_efield_fieldsolve.restype = C.c_int32
+    L.mq_cube_fields.argtypes = [P(mq_cube_geom), C.c_double, C.c_double, C.c_double, C.c_int32, P(C.c_int32),
+                                 P(C.c_double), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, P(mq_solve_stats)]
+    L.mq_cube_fields.restype = C.c_int32
+    L.mq_cube_dc_combined.argtypes = [C.c_size_t, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double,
+                                      C.c_double, C.c_double, C.c_void_p]
+    L.mq_cube_dc_combined.restype = C.c_int32
+    L.mq_tandem_create.argtypes = [P(mq_tandem_desc), C.c_int32, P(C.c_void_p)]
+    L.mq_tandem_create.restype = C.c_int32
+    L.mq_tandem_destroy.argtypes = [C.c_void_p]
+    L.mq_tandem_destroy.restype = None
+    L.mq_tandem_last_error.argtypes = [C.c_void_p]
+    L.mq_tandem_last_error.restype = C.c_char_p
+    L.mq_tandem_layout.argtypes = [P(mq_tandem_desc), P(C.c_double), P(C.c_double), P(C.c_double)]
+    L.mq_tandem_layout.restype = C.c_int32
+    L.mq_tandem_inject.argtypes = [P(mq_tandem_desc), C.c_uint64, C.c_int32, P(mq_tracks), C.c_size_t]
+    L.mq_tandem_inject.restype = C.c_int32
+    L.mq_tandem_advance.argtypes = [C.c_void_p, P(mq_tracks), C.c_size_t, C.c_uint64, C.c_uint64, P(mq_port_counts),
+                                    P(C.c_double)]
+    L.mq_tandem_advance.restype = C.c_int32
+    L.mq_tandem_frame.argtypes = [P(mq_tracks), C.c_size_t, P(mq_tandem_frame_counts)]
+    L.mq_tandem_frame.restype = C.c_int32
 
 
 def _declare_engine(L) -> None:

@@ -14,12 +14,13 @@ OUT = HERE / "_ref" / "libmqref.so"
 
 def build() -> Path:
     OUT.parent.mkdir(exist_ok=True)
-    src = HERE / "mqref.c"
-    if OUT.exists() and OUT.stat().st_mtime > max(src.stat().st_mtime, (HERE / "mqref.h").stat().st_mtime):
+    srcs = [HERE / "mqref.c", HERE / "mqtandem.c"]
+    deps = srcs + [HERE / "mqref.h", HERE / "mqtandem.h"]
+    if OUT.exists() and OUT.stat().st_mtime > max(p.stat().st_mtime for p in deps):
         return OUT
     tmp = OUT.with_suffix(".tmp.so")
     subprocess.run(["gcc", "-O2", "-std=c11", "-Wall", "-ffp-contract=off", "-fPIC", "-pthread", "-shared",
-                    str(src), "-o", str(tmp), "-lm"], check=True, capture_output=True)
+                    *map(str, srcs), "-o", str(tmp), "-lm"], check=True, capture_output=True)
     tmp.replace(OUT)
     return OUT
 
