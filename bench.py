@@ -178,6 +178,163 @@ def run_reference(args, rank: int, world: int):
     print(json.dumps(line), flush=True)
 
 
+TANDEM_METRIC = "track-steps/s, 1 GB300: nine-channel tandem transport (FP64 kernel, bit-exact with the CPU oracle)"
+TANDEM_UNIT = "track-steps/s"
+# algorithmic bytes per track-step: 8 corner nodes x float4 (16 B) x the fields the region reads
+TANDEM_BYTES = {"cube": 8 * 16 * 2, "port": 8 * 16 * 3, "idle": 8 * 16 * 4}
+
+
+def tandem_setup(args):
+    """The tandem workload: Fig. 5 drives (tones 39 / 47 / 53 / 59.25 kHz on four ports, five
+    idle ports gated +4 V), ubiquitin 6+..10+ mixture, tracks launched at the nine mouths, cube at
+    0.51875 mm, the nine ports on the calibrated S14 channel grid at ``--port-h`` mm, each port
+    holding its own device-resident copy of that grid unless ``--tandem-shared``."""
+    import multiq_workbench_gb300 as mq
+    h = float(args.port_h)
+    ch = mq.Fields.build(mq.Geom.s14(h_mm=h, n_xy=int(round(16.0 / h))))
+    pg = mq.PortGrid.from_fields(ch)
+    grids = [pg] * 9 if args.tandem_shared else [pg] + [pg.replica() for _ in range(8)]
+    m = mq.TandemModel(mq.DEFAULT_TONES, n=args.tracks, seed=486, fine=True, mouth_start=True, port_grids=grids)
+    wl = (f"tandem: {args.tracks:,} tracks at the nine mouths, Fig. 5 tones, ubiquitin 6+..10+, cube 0.51875 mm "
+          f"{'x'.join(map(str, m.cube.dims))}, ports on S14 {h:g} mm {ch.nx}x{ch.ny}x{ch.nz} "
+          f"({'one shared grid' if args.tandem_shared else 'nine device-resident copies'}), "
+          f"{args.tandem_steps} global steps per bench step")
+    return m, wl
+
+
+def tandem_bytes(st) -> float:
+    return (TANDEM_BYTES["cube"] * st.steps_cube + TANDEM_BYTES["port"] * st.steps_port
+            + TANDEM_BYTES["idle"] * st.steps_idle)
+
+
+def tandem_cpu(m, pulse, steps: int, target_s: float, threads: int) -> dict:
+    """The tandem oracle on the first k tracks of the pulse for the same global steps, k grown
+    until the run takes about ``target_s``."""
+    from oracle import mqtandem as O
+    d = O.desc_from(m.desc)
+    k = min(pulse.n, 2048)
+    while True:
+        s = O.State(k)
+        for name, _ in O.TRACK_FIELDS:
+            getattr(s, name)[:] = getattr(pulse, name)[:k]
+        ns = np.zeros(3, np.uint64)
+        t0 = time.perf_counter()
+        O.advance(d, s, 0, steps, threads=threads, nsteps=ns)
+        dt = time.perf_counter() - t0
+        if dt >= 0.3 * target_s or k >= pulse.n:
+            return {"value": float(ns.sum()) / dt, "track_steps": int(ns.sum()), "seconds": dt, "tracks": k}
+        k = int(min(pulse.n, k * max(2.0, target_s / max(dt, 1e-3))))
+
+
+def run_tandem(args, rank: int, world: int):
+    import multiq_workbench_gb300 as mq
+    threads = os.cpu_count() or 1
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        m, wl = tandem_setup(args)
+        pulse = m.tracks.copy()
+        vals = []
+        r = None
+        for _ in range(max(0, args.warmup)):
+            tandem_cpu(m, pulse, min(args.tandem_steps, 200), 1.0, threads)
+        t_all = time.perf_counter()
+        for _ in range(args.steps):
+            r = tandem_cpu(m, pulse, args.tandem_steps, 10.0, threads)
+            vals.append(r["value"])
+        wall = time.perf_counter() - t_all
+        v = float(np.median(vals))
+        smp = f"first {r['tracks']} tracks of the pulse for {args.tandem_steps} steps ({r['seconds']:.1f} s)"
+        print(json.dumps({"impl": "reference", "metric": TANDEM_METRIC, "value": v, "unit": TANDEM_UNIT, "n_gpus": world,
+                          "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall / max(1, args.steps),
+                          "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                          "data": "synthetic", "config": {"workload": wl, "sample": smp},
+                          "cpu_baseline": {"value": v, "unit": TANDEM_UNIT, "cores": threads, "kind": "port", "sample": smp},
+                          "e2e": {"value": v, "unit": TANDEM_UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}),
+              flush=True)
+        return
+    import torch
+    import __graft_entry__ as ge
+    ge.build()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    m, wl = tandem_setup(args)
+    m.device = local
+    pulse = m.tracks.copy()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+
+    def one():
+        m.tracks = pulse.copy()
+        m.step = 0
+        m.counts = type(m.counts)()
+        t0 = time.perf_counter()
+        st = m.advance(args.tandem_steps)
+        return st, time.perf_counter() - t0
+
+    for _ in range(args.warmup):
+        one()
+    clocks = Clocks(local)
+    clocks.start()
+    sts, walls = [], []
+    torch.cuda.synchronize()
+    for _ in range(args.steps):
+        flush_l2(flush)
+        torch.cuda.synchronize()
+        st, w = one()
+        sts.append(st)
+        walls.append(w)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ts = sum(s.track_steps for s in sts)
+    t_dev = sum(s.kernel_ms for s in sts) * 1e-3
+    t_wall = sum(walls)
+    ts_all = float(ts)
+    if world > 1:   # replicas: every rank runs its own pulse; whole-job rate over the slowest rank
+        import torch.distributed as dist
+        tt = torch.tensor([t_dev, t_wall], dtype=torch.float64, device=f"cuda:{local}")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        sv = torch.tensor([ts_all], dtype=torch.float64, device=f"cuda:{local}")
+        dist.all_reduce(sv, op=dist.ReduceOp.SUM)
+        t_dev, t_wall, ts_all = float(tt[0]), float(tt[1]), float(sv[0])
+    value = ts_all / t_dev
+    e2e = ts_all / t_wall
+    if rank != 0:
+        m.close()
+        return
+    peaks = measured_peaks()
+    hbm = peaks.get("hbm_gbs") or 6800.0
+    achieved = sum(tandem_bytes(s) for s in sts) / (sum(s.kernel_ms for s in sts) * 1e-3) / 1e9
+    f = m.frame()
+    cnt = m.counts_array()
+    cpu = None
+    if not args.no_cpu:
+        r = tandem_cpu(m, pulse, args.tandem_steps, 12.0, threads)
+        cpu = {"value": r["value"], "unit": TANDEM_UNIT, "cores": threads, "kind": "port",
+               "sample": f"first {r['tracks']} tracks of the pulse for {args.tandem_steps} steps ({r['seconds']:.1f} s)"}
+    last = sts[-1]
+    line = {"metric": TANDEM_METRIC, "value": value, "unit": TANDEM_UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": wl, "tracks": args.tracks, "global_steps": args.tandem_steps,
+                       "l2_flush": "256 MB write before every timed step"},
+            "track_steps_per_step": ts / args.steps,
+            "e2e": {"value": e2e, "unit": TANDEM_UNIT, "h2d_bytes_per_step": int(last.h2d_bytes),
+                    "d2h_bytes_per_step": int(last.d2h_bytes)},
+            "gpu_launches": int(sum(s.launches for s in sts)),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                         "traffic": None, "peak_source": "measured hbm_gbs" if peaks.get("hbm_gbs") else "fallback",
+                         "kernel": "k_tandem", "algorithmic_bytes_per_track_step": TANDEM_BYTES},
+            "cpu_baseline": cpu, "clocks": clk,
+            "census": {"split": f.split, "channel": f.channel, "combine": f.combine, "lost": f.lost, "back": f.back,
+                       "detected": f.detected},
+            "ports": {"entered": cnt[:, 0].tolist(), "returned": cnt[:, 1].tolist(), "forwarded": cnt[:, 2].tolist(),
+                      "revisits": int(cnt[:, 3].sum()), "from_other": int(cnt[:, 4].sum()),
+                      "retry_matrix": cnt[:, 5:14].tolist(), "reverse_entries": int(cnt[:, 14].sum()),
+                      "lost": cnt[:, 15].tolist(), "by_charge": cnt[:, 16:21].sum(0).tolist()}}
+    print(json.dumps(line), flush=True)
+    m.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -189,6 +346,12 @@ def main():
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--ions-per-job", type=int, default=256,
                     help="ions per job (256 = the benchmark workload; smaller = a profiling case)")
+    ap.add_argument("--workload", default="sweep", choices=["sweep", "tandem"],
+                    help="sweep: the batched channel sweep (default); tandem: the nine-channel tandem transport")
+    ap.add_argument("--tracks", type=int, default=1 << 20, help="tandem: tracks in the pulse")
+    ap.add_argument("--tandem-steps", type=int, default=1000, help="tandem: global steps per bench step")
+    ap.add_argument("--port-h", type=float, default=0.05, help="tandem: port grid spacing [mm]")
+    ap.add_argument("--tandem-shared", action="store_true", help="tandem: the nine ports share one device grid")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
@@ -199,6 +362,12 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl" if args.impl == "gb300" else "gloo")
+    if args.workload == "tandem":
+        run_tandem(args, rank, world)
+        if dist:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
     if args.impl == "reference":
         run_reference(args, rank, world)
         if dist:

@@ -122,10 +122,19 @@ const char* mq_tandem_last_error(mq_tandem* t);
 mq_status mq_tandem_layout(const mq_tandem_desc* d, double* seam_m, double* size_m, double mouths_m[18]);
 /* launch n tracks as Model::new does (mouth_start: at the nine mouths, else through the entrance) */
 mq_status mq_tandem_inject(const mq_tandem_desc* d, uint64_t seed, int32_t mouth_start, mq_tracks* out, size_t n);
+/* What one advance executed: track-steps by region kind (splitter/combiner cube, driven port,
+ * idle port), kernel time and launches, and the bytes copied each way. */
+typedef struct mq_tandem_stats {
+    uint64_t steps_cube, steps_port, steps_idle;
+    double kernel_ms;
+    uint32_t launches, pad;
+    uint64_t h2d_bytes, d2h_bytes;
+} mq_tandem_stats;
+
 /* advance tracks (host arrays, in place) by `steps` global steps starting at global step
- * step0; counts[9] accumulate.  Synchronous. */
+ * step0; counts[9] accumulate; stats may be NULL.  Synchronous. */
 mq_status mq_tandem_advance(mq_tandem* t, mq_tracks* tr, size_t n, uint64_t step0, uint64_t steps,
-                            mq_port_counts counts[9], double* device_ms);
+                            mq_port_counts counts[9], mq_tandem_stats* stats);
 mq_status mq_tandem_frame(const mq_tracks* tr, size_t n, mq_tandem_frame_counts* out);
 
 #ifdef __cplusplus

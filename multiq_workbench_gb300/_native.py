@@ -142,6 +142,12 @@ class mq_port_counts(C.Structure):
                 ("reverse_entries", C.c_uint32), ("lost", C.c_uint32), ("by_charge", C.c_uint32 * 5)]
 
 
+class mq_tandem_stats(C.Structure):
+    _fields_ = [("steps_cube", C.c_uint64), ("steps_port", C.c_uint64), ("steps_idle", C.c_uint64),
+                ("kernel_ms", C.c_double), ("launches", C.c_uint32), ("pad", C.c_uint32), ("h2d_bytes", C.c_uint64),
+                ("d2h_bytes", C.c_uint64)]
+
+
 class mq_tandem_frame_counts(C.Structure):
     _fields_ = [(k, C.c_uint64) for k in ("split", "channel", "combine", "lost", "back", "detected")]
 
@@ -222,7 +228,7 @@ def _declare_tandem(L) -> None:
     L.mq_tandem_inject.argtypes = [P(mq_tandem_desc), C.c_uint64, C.c_int32, P(mq_tracks), C.c_size_t]
     L.mq_tandem_inject.restype = C.c_int32
     L.mq_tandem_advance.argtypes = [C.c_void_p, P(mq_tracks), C.c_size_t, C.c_uint64, C.c_uint64, P(mq_port_counts),
-                                    P(C.c_double)]
+                                    P(mq_tandem_stats)]
     L.mq_tandem_advance.restype = C.c_int32
     L.mq_tandem_frame.argtypes = [P(mq_tracks), C.c_size_t, P(mq_tandem_frame_counts)]
     L.mq_tandem_frame.restype = C.c_int32

@@ -143,94 +143,117 @@ __device__ void collide(double v[3], uint64_t* rng, const TSpec& s, double s_gas
     }
 }
 
-__global__ void __launch_bounds__(128) k_tandem(TConst C, Tracks T, uint32_t n, const double* __restrict__ drive,
-                                                uint32_t steps, uint32_t* __restrict__ counts) {
-    const uint32_t id = blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= n) return;
-    int reg = T.region[id];
-    if (reg >= R_LOST) return;
-    double x[3] = {T.x[id], T.y[id], T.z[id]};
-    double v[3] = {T.vx[id], T.vy[id], T.vz[id]};
-    uint64_t rng = T.rng[id];
-    const int sp = T.sp[id];
-    int last = T.last[id];
-    const TSpec S = C.sp[sp];
-    for (uint32_t k = 0; k < steps && reg < R_LOST; ++k) {
-        const double* dr = drive + (size_t)k * 10;   // rf, ac[0..9)
-        const double rf = dr[0];
-        double e[3];
-        if (reg == R_SPLIT || reg == R_COMBINE) cube_field(C, C.cdc[reg == R_COMBINE ? 1 : 0], x, rf, e);
-        else { const int i = reg - 1; chan_field(C.port[i], C.gate_v, x, rf, dr[1 + i], e); }
-        // transport_step (lib.rs:90-103)
-        for (int d = 0; d < 3; ++d) {
-            v[d] += S.qmdt * e[d];
-            x[d] += v[d] * C.dt;
-        }
-        collide(v, &rng, S, C.s_gas);
-        if (reg == R_SPLIT || reg == R_COMBINE) {
-            const double mm[3] = {x[0] * 1000.0, x[1] * 1000.0, x[2] * 1000.0};
-            int sg = 0;
-            if (mqc::classify(C.cube, mm, 0.0, &sg) != mqc::ID_FREE) { reg = R_LOST; continue; }
-            if (x[2] > C.seam) {
-                const int i = mqc::nearest_port(C.cube, mm[0], mm[1]);
-                const double* c = C.mouth[i];
-                if (mqc::dist2d(x[0] - c[0], x[1] - c[1]) < C.ap_r * 0.001) {
-                    // enter (lib.rs:338-367)
-                    uint32_t* cnt = counts + (size_t)i * kNC;
-                    x[0] += C.axis - c[0];
-                    x[1] += C.axis - c[1];
-                    const double depth = x[2] - C.seam;
-                    if (reg == R_SPLIT) {
-                        x[2] = Z_RETURN + depth;
-                        atomicAdd(cnt + 0, 1u);
-                        if (last >= 0) {
-                            atomicAdd(cnt + 3, 1u);
-                            atomicAdd(cnt + 5 + last, 1u);
-                            if (last != i) atomicAdd(cnt + 4, 1u);
-                        }
-                    } else {
-                        x[2] = Z_EXIT - depth;
-                        v[2] *= -1.0;
-                        atomicAdd(cnt + 14, 1u);
-                    }
-                    reg = 1 + i;
-                    continue;
-                }
-                if (x[2] > C.size) { reg = R_LOST; continue; }
-            }
-            if (x[1] > C.size) {
-                if (mqc::dist2d(mm[0] - C.ent_c, mm[2] - C.ent_b) >= C.ap_r) { reg = R_LOST; continue; }
-            }
-            if (x[1] > C.size + C.l_ext_m) reg = (reg == R_SPLIT) ? R_BACK : R_DETECTED;
-            else if (x[0] < 0.0 || x[1] < 0.0 || x[2] < 0.0 || x[0] > C.size) reg = R_LOST;
-        } else {
-            const int i = reg - 1;
-            uint32_t* cnt = counts + (size_t)i * kNC;
-            if (chan_crash(C.port[i], x)) { reg = R_LOST; atomicAdd(cnt + 15, 1u); }
-            else if (x[2] < Z_RETURN || x[2] > Z_EXIT) {
-                // leave (lib.rs:368-385)
-                const double* c = C.mouth[i];
-                x[0] += c[0] - C.axis;
-                x[1] += c[1] - C.axis;
-                if (x[2] < Z_RETURN) {
-                    x[2] = C.seam + x[2] - Z_RETURN;
-                    reg = R_SPLIT;
-                    last = i;
-                    atomicAdd(cnt + 1, 1u);
-                } else {
-                    x[2] = C.seam - (x[2] - Z_EXIT);
-                    v[2] *= -1.0;
-                    reg = R_COMBINE;
-                    last = -1;
-                    atomicAdd(cnt + 2, 1u);
-                    atomicAdd(cnt + 16 + sp, 1u);
-                }
-            }
-        }
+// Executed track-steps by region kind (cube, driven port, idle port): one warp-reduced atomic per warp.
+__device__ __forceinline__ void add_steps(unsigned long long* st, uint32_t c, uint32_t p, uint32_t q) {
+    c = __reduce_add_sync(0xffffffffu, c);
+    p = __reduce_add_sync(0xffffffffu, p);
+    q = __reduce_add_sync(0xffffffffu, q);
+    if ((threadIdx.x & 31) == 0) {
+        if (c) atomicAdd(st + 0, (unsigned long long)c);
+        if (p) atomicAdd(st + 1, (unsigned long long)p);
+        if (q) atomicAdd(st + 2, (unsigned long long)q);
     }
-    T.x[id] = x[0]; T.y[id] = x[1]; T.z[id] = x[2];
-    T.vx[id] = v[0]; T.vy[id] = v[1]; T.vz[id] = v[2];
-    T.rng[id] = rng; T.region[id] = reg; T.last[id] = last;
+}
+
+// blockDim.x is a multiple of 32 and no lane returns early, so the warp reductions see full warps.
+__global__ void __launch_bounds__(128) k_tandem(TConst C, Tracks T, uint32_t n, const double* __restrict__ drive,
+                                                uint32_t steps, uint32_t* __restrict__ counts,
+                                                unsigned long long* __restrict__ stepc) {
+    const uint32_t id = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t n_cube = 0, n_port = 0, n_idle = 0;
+    if (id < n && T.region[id] < R_LOST) {
+        int reg = T.region[id];
+        double x[3] = {T.x[id], T.y[id], T.z[id]};
+        double v[3] = {T.vx[id], T.vy[id], T.vz[id]};
+        uint64_t rng = T.rng[id];
+        const int sp = T.sp[id];
+        int last = T.last[id];
+        const TSpec S = C.sp[sp];
+        for (uint32_t k = 0; k < steps && reg < R_LOST; ++k) {
+            const double* dr = drive + (size_t)k * 10;   // rf, ac[0..9)
+            const double rf = dr[0];
+            double e[3];
+            if (reg == R_SPLIT || reg == R_COMBINE) {
+                cube_field(C, C.cdc[reg == R_COMBINE ? 1 : 0], x, rf, e);
+                ++n_cube;
+            } else {
+                const int i = reg - 1;
+                chan_field(C.port[i], C.gate_v, x, rf, dr[1 + i], e);
+                if (C.port[i].idle) ++n_idle;
+                else ++n_port;
+            }
+            // transport_step (lib.rs:90-103)
+            for (int d = 0; d < 3; ++d) {
+                v[d] += S.qmdt * e[d];
+                x[d] += v[d] * C.dt;
+            }
+            collide(v, &rng, S, C.s_gas);
+            if (reg == R_SPLIT || reg == R_COMBINE) {
+                const double mm[3] = {x[0] * 1000.0, x[1] * 1000.0, x[2] * 1000.0};
+                int sg = 0;
+                if (mqc::classify(C.cube, mm, 0.0, &sg) != mqc::ID_FREE) { reg = R_LOST; continue; }
+                if (x[2] > C.seam) {
+                    const int i = mqc::nearest_port(C.cube, mm[0], mm[1]);
+                    const double* c = C.mouth[i];
+                    if (mqc::dist2d(x[0] - c[0], x[1] - c[1]) < C.ap_r * 0.001) {
+                        // enter (lib.rs:338-367)
+                        uint32_t* cnt = counts + (size_t)i * kNC;
+                        x[0] += C.axis - c[0];
+                        x[1] += C.axis - c[1];
+                        const double depth = x[2] - C.seam;
+                        if (reg == R_SPLIT) {
+                            x[2] = Z_RETURN + depth;
+                            atomicAdd(cnt + 0, 1u);
+                            if (last >= 0) {
+                                atomicAdd(cnt + 3, 1u);
+                                atomicAdd(cnt + 5 + last, 1u);
+                                if (last != i) atomicAdd(cnt + 4, 1u);
+                            }
+                        } else {
+                            x[2] = Z_EXIT - depth;
+                            v[2] *= -1.0;
+                            atomicAdd(cnt + 14, 1u);
+                        }
+                        reg = 1 + i;
+                        continue;
+                    }
+                    if (x[2] > C.size) { reg = R_LOST; continue; }
+                }
+                if (x[1] > C.size) {
+                    if (mqc::dist2d(mm[0] - C.ent_c, mm[2] - C.ent_b) >= C.ap_r) { reg = R_LOST; continue; }
+                }
+                if (x[1] > C.size + C.l_ext_m) reg = (reg == R_SPLIT) ? R_BACK : R_DETECTED;
+                else if (x[0] < 0.0 || x[1] < 0.0 || x[2] < 0.0 || x[0] > C.size) reg = R_LOST;
+            } else {
+                const int i = reg - 1;
+                uint32_t* cnt = counts + (size_t)i * kNC;
+                if (chan_crash(C.port[i], x)) { reg = R_LOST; atomicAdd(cnt + 15, 1u); }
+                else if (x[2] < Z_RETURN || x[2] > Z_EXIT) {
+                    // leave (lib.rs:368-385)
+                    const double* c = C.mouth[i];
+                    x[0] += c[0] - C.axis;
+                    x[1] += c[1] - C.axis;
+                    if (x[2] < Z_RETURN) {
+                        x[2] = C.seam + x[2] - Z_RETURN;
+                        reg = R_SPLIT;
+                        last = i;
+                        atomicAdd(cnt + 1, 1u);
+                    } else {
+                        x[2] = C.seam - (x[2] - Z_EXIT);
+                        v[2] *= -1.0;
+                        reg = R_COMBINE;
+                        last = -1;
+                        atomicAdd(cnt + 2, 1u);
+                        atomicAdd(cnt + 16 + sp, 1u);
+                    }
+                }
+            }
+        }
+        T.x[id] = x[0]; T.y[id] = x[1]; T.z[id] = x[2];
+        T.vx[id] = v[0]; T.vy[id] = v[1]; T.vz[id] = v[2];
+        T.rng[id] = rng; T.region[id] = reg; T.last[id] = last;
+    }
+    add_steps(stepc, n_cube, n_port, n_idle);
 }
 
 }  // namespace
@@ -246,6 +269,7 @@ struct mq_tandem {
     void* drive = nullptr;
     size_t drive_cap = 0;
     uint32_t* counts = nullptr;
+    unsigned long long* stepc = nullptr;   // executed track-steps: cube, driven port, idle port
     cudaStream_t st = nullptr;
     cudaEvent_t ev[2] = {nullptr, nullptr};
 };
@@ -329,6 +353,7 @@ mq_status mq_tandem_create(const mq_tandem_desc* d, int32_t device, mq_tandem** 
         P.idle = p.tone_khz == 0.0;
     }
     if (cudaMalloc(&t->counts, 9 * kNC * sizeof(uint32_t)) != cudaSuccess) return bail(MQ_ERR_NOMEM);
+    if (cudaMalloc(&t->stepc, 3 * sizeof(unsigned long long)) != cudaSuccess) return bail(MQ_ERR_NOMEM);
     C.cube = d->cube;
     for (int a = 0; a < 3; ++a) { C.cn[a] = d->cube_dims[a]; C.clo[a] = d->cube_lo_mm[a]; }
     C.ch_mm = d->cube_h_mm;
@@ -366,6 +391,7 @@ void mq_tandem_destroy(mq_tandem* t) {
     if (t->tr) cudaFree(t->tr);
     if (t->drive) cudaFree(t->drive);
     if (t->counts) cudaFree(t->counts);
+    if (t->stepc) cudaFree(t->stepc);
     for (auto& e : t->ev) if (e) cudaEventDestroy(e);
     if (t->st) cudaStreamDestroy(t->st);
     delete t;
@@ -374,7 +400,7 @@ void mq_tandem_destroy(mq_tandem* t) {
 const char* mq_tandem_last_error(mq_tandem* t) { return t ? t->err.c_str() : "null tandem"; }
 
 mq_status mq_tandem_advance(mq_tandem* t, mq_tracks* tr, size_t n, uint64_t step0, uint64_t steps, mq_port_counts counts[9],
-                            double* device_ms) {
+                            mq_tandem_stats* stats) {
     if (!t || !tr || !counts) return MQ_ERR_INVALID;
     if (n > 0xFFFFFFF0ull) return tfail(t, MQ_ERR_TOO_LARGE, "at most 2^32-16 tracks");
     TCK(cudaSetDevice(t->dev), "cudaSetDevice");
@@ -407,34 +433,56 @@ mq_status mq_tandem_advance(mq_tandem* t, mq_tracks* tr, size_t n, uint64_t step
     std::vector<uint32_t> cnt(9 * kNC);
     for (int i = 0; i < 9; ++i) std::memcpy(&cnt[(size_t)i * kNC], &counts[i], sizeof(mq_port_counts));
     TCK(cudaMemcpyAsync(t->counts, cnt.data(), cnt.size() * 4, cudaMemcpyHostToDevice, t->st), "counter upload");
-    const uint64_t chunk = 4096;
-    if (t->drive_cap < chunk * 10 * 8) {
+    TCK(cudaMemsetAsync(t->stepc, 0, 3 * sizeof(unsigned long long), t->st), "step counters");
+    // Drive table: up to kTab steps per upload; kernels of `per` steps each, about 2^27 track-steps
+    // per launch so that no single launch runs for long.
+    const uint64_t kTab = 65536;
+    const uint64_t tab = steps < kTab ? (steps ? steps : 1) : kTab;
+    if (t->drive_cap < tab * 10 * 8) {
         if (t->drive) cudaFree(t->drive);
         t->drive = nullptr; t->drive_cap = 0;
-        TCK(cudaMalloc(&t->drive, chunk * 10 * 8), "drive table");
-        t->drive_cap = chunk * 10 * 8;
+        TCK(cudaMalloc(&t->drive, tab * 10 * 8), "drive table");
+        t->drive_cap = tab * 10 * 8;
     }
-    std::vector<double> dtab(chunk * 10);
-    float ms_total = 0.0f;
-    for (uint64_t s = 0; s < steps; s += chunk) {
-        const uint64_t k = steps - s < chunk ? steps - s : chunk;
+    uint64_t per = n ? ((uint64_t)1 << 27) / n : tab;
+    per = per < 32 ? 32 : (per > 4096 ? 4096 : per);
+    std::vector<double> dtab(tab * 10);
+    uint32_t launches = 0;
+    uint64_t h2d = tb + cnt.size() * 4;
+    for (uint64_t s = 0; s < steps || s == 0; s += tab) {
+        const uint64_t k = steps - s < tab ? steps - s : tab;
         drive_table(t->desc, step0 + s, k, dtab.data());
-        TCK(cudaMemcpyAsync(t->drive, dtab.data(), k * 10 * 8, cudaMemcpyHostToDevice, t->st), "drive upload");
-        TCK(cudaEventRecord(t->ev[0], t->st), "event");
-        if (n) k_tandem<<<(unsigned)((n + 127) / 128), 128, 0, t->st>>>(t->C, T, (uint32_t)n, (const double*)t->drive,
-                                                                        (uint32_t)k, t->counts);
-        TCK(cudaGetLastError(), "tandem kernel");
-        TCK(cudaEventRecord(t->ev[1], t->st), "event");
-        TCK(cudaStreamSynchronize(t->st), "tandem kernel");   // the host drive buffer is reused next chunk
-        float ms = 0.0f;
-        cudaEventElapsedTime(&ms, t->ev[0], t->ev[1]);
-        ms_total += ms;
+        // pageable source: the call returns once the host buffer has been staged, so it may be refilled next
+        if (k) TCK(cudaMemcpyAsync(t->drive, dtab.data(), k * 10 * 8, cudaMemcpyHostToDevice, t->st), "drive upload");
+        h2d += k * 10 * 8;
+        if (s == 0) TCK(cudaEventRecord(t->ev[0], t->st), "event");   // times the kernels (and later table blocks)
+        if (!steps) break;
+        for (uint64_t q = 0; q < k && n; q += per, ++launches) {
+            const uint64_t m = k - q < per ? k - q : per;
+            k_tandem<<<(unsigned)((n + 127) / 128), 128, 0, t->st>>>(t->C, T, (uint32_t)n, (const double*)t->drive + q * 10,
+                                                                    (uint32_t)m, t->counts, t->stepc);
+            TCK(cudaGetLastError(), "tandem kernel");
+        }
     }
+    TCK(cudaEventRecord(t->ev[1], t->st), "event");
     for (int k = 0; k < 10; ++k) TCK(cudaMemcpyAsync(host[k], dev[k], sz[k] * n, cudaMemcpyDeviceToHost, t->st), "track download");
     TCK(cudaMemcpyAsync(cnt.data(), t->counts, cnt.size() * 4, cudaMemcpyDeviceToHost, t->st), "counter download");
+    unsigned long long sc[3] = {0, 0, 0};
+    TCK(cudaMemcpyAsync(sc, t->stepc, sizeof(sc), cudaMemcpyDeviceToHost, t->st), "step counters");
     TCK(cudaStreamSynchronize(t->st), "tandem");
     for (int i = 0; i < 9; ++i) std::memcpy(&counts[i], &cnt[(size_t)i * kNC], sizeof(mq_port_counts));
-    if (device_ms) *device_ms = ms_total;
+    if (stats) {
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, t->ev[0], t->ev[1]);
+        std::memset(stats, 0, sizeof(*stats));
+        stats->steps_cube = sc[0];
+        stats->steps_port = sc[1];
+        stats->steps_idle = sc[2];
+        stats->kernel_ms = ms;
+        stats->launches = launches;
+        stats->h2d_bytes = h2d;
+        stats->d2h_bytes = tb + cnt.size() * 4 + sizeof(sc);
+    }
     return MQ_OK;
 }
 

@@ -5,8 +5,8 @@ Python mirror of ``trapsim::Model`` (simulation/trapsim/src/lib.rs:55-336): ``Ta
 n, seed, fine, mouth_start)`` builds the cube geometry and fields (``Geometry::as_built`` with the
 3x3 port array, snapped to 1.04 / 0.52 mm), the calibrated channel world and the Fig. 5 ubiquitin
 mixture, launches the tracks; ``advance(steps)`` and ``frame()`` behave as the reference's.
-Each port may carry its own channel grid (``port_fields``); by default the nine ports share one,
-as in the reference.
+Each port may carry its own channel grid (``port_fields`` / ``port_grids``); by default the nine
+ports share one, as in the reference.
 """
 from __future__ import annotations
 
@@ -286,6 +286,27 @@ class Frame:
     seam_mm: float
 
 
+@dataclass
+class TandemStats:
+    """Executed track-steps by region kind, kernel time, launches and copies of one advance."""
+    steps_cube: int
+    steps_port: int
+    steps_idle: int
+    kernel_ms: float
+    launches: int
+    h2d_bytes: int
+    d2h_bytes: int
+
+    @property
+    def track_steps(self) -> int:
+        return self.steps_cube + self.steps_port + self.steps_idle
+
+    @classmethod
+    def from_native(cls, s: N.mq_tandem_stats) -> "TandemStats":
+        return cls(int(s.steps_cube), int(s.steps_port), int(s.steps_idle), float(s.kernel_ms), int(s.launches),
+                   int(s.h2d_bytes), int(s.d2h_bytes))
+
+
 # ---------------------------------------------------------------------------------------- model
 
 
@@ -297,17 +318,43 @@ def _check_t(code: int, what: str, h) -> None:
         raise N.MqError(code, what, detail)
 
 
+@dataclass
+class PortGrid:
+    """What one port reads: its channel grid's RF (w = conductor mask), AC, combined DC and gate
+    plate basis, float32 (n, 4) each (the packed ``World`` of world.rs:141-160)."""
+    nx: int
+    ny: int
+    nz: int
+    h: float
+    rf: np.ndarray
+    ac: np.ndarray
+    dc: np.ndarray
+    gate: np.ndarray
+    axis_mm: float
+    q1_start_mm: float
+
+    @classmethod
+    def from_fields(cls, f: Fields, dc_cal=DC_CAL) -> "PortGrid":
+        return cls(f.nx, f.ny, f.nz, f.h, f.rf, f.ac, f.dc_field(dc_cal), f.dc[1], f.geom.axis(), f.geom.q1_start)
+
+    def replica(self) -> "PortGrid":
+        """The same grid in arrays of its own (a port with a device-resident grid of its own)."""
+        return PortGrid(self.nx, self.ny, self.nz, self.h, self.rf.copy(), self.ac.copy(), self.dc.copy(),
+                        self.gate.copy(), self.axis_mm, self.q1_start_mm)
+
+
 class TandemModel:
     """``trapsim::Model`` on the GB300 (lib.rs:106-336).
 
     ``channel``: channel basis fields (default: the calibrated S14 world, ``Geom.s14()``) shared
-    by the nine ports unless ``port_fields`` (nine ``Fields``) gives each port its own grid.
+    by the nine ports unless ``port_fields`` (nine ``Fields``) or ``port_grids`` (nine
+    ``PortGrid``) give ports grids of their own; arrays shared between ports are uploaded once.
     ``cube_h``: cube grid spacing target in mm (default 0.52 fine / 1.04 coarse)."""
 
     def __init__(self, tones=DEFAULT_TONES, n: int = 180, seed: int = 486, fine: bool = False,
                  mouth_start: bool = True, *, channel: Fields | None = None, port_fields=None,
-                 cube_h: float | None = None, preset: TandemPreset | None = None, device: int = 0,
-                 dc_cal=DC_CAL, cube_tol: float = 1e-7):
+                 port_grids=None, cube_h: float | None = None, preset: TandemPreset | None = None,
+                 device: int = 0, dc_cal=DC_CAL, cube_tol: float = 1e-7):
         self.tones = tuple(float(t) for t in tones)
         assert len(self.tones) == 9
         self.preset = preset or TandemPreset.fig5()
@@ -316,19 +363,20 @@ class TandemModel:
         self.geom, self.cube_h = g.snap(cube_h if cube_h is not None else (0.52 if fine else 1.04))
         self.cube = CubeFields.build(self.geom, self.cube_h, 0.4, cube_tol)
         self.dc = [self.cube.dc_combined(20.0, 20.1, 20.5, 18.0), self.cube.dc_combined(15.0, 15.1, 14.8, 15.0)]
-        if port_fields is None:
-            ch = channel if channel is not None else Fields.build(Geom.s14())
-            port_fields = [ch] * 9
-        assert len(port_fields) == 9
-        self.port_fields = list(port_fields)
-        # combined DC per distinct grid (ports sharing a grid share the array)
-        self._port_dc = {}
-        for f in self.port_fields:
-            if id(f) not in self._port_dc:
-                self._port_dc[id(f)] = f.dc_field(dc_cal)
+        if port_grids is None:
+            if port_fields is None:
+                port_fields = [channel if channel is not None else Fields.build(Geom.s14())] * 9
+            assert len(port_fields) == 9
+            made = {}   # one PortGrid per distinct Fields: ports sharing a grid share its arrays
+            for f in port_fields:
+                if id(f) not in made:
+                    made[id(f)] = PortGrid.from_fields(f, dc_cal)
+            port_grids = [made[id(f)] for f in port_fields]
+        assert len(port_grids) == 9
+        self.port_grids = list(port_grids)
         self.desc = self._make_desc()
         self.seam, self.size, self.mouth = self.layout()
-        self.axis = self.port_fields[0].geom.axis() * 1e-3
+        self.axis = self.port_grids[0].axis_mm * 1e-3
         self.tracks = Tracks(n)
         t = self.tracks.native()
         N.check(N.lib().mq_tandem_inject(C.byref(self.desc), C.c_uint64(seed), 1 if mouth_start else 0, C.byref(t), n),
@@ -355,17 +403,14 @@ class TandemModel:
         d.cube_h_mm = self.cube_h
         d.cube_rf4 = self.cube.rf.ctypes.data
         d.cube_dc4[0], d.cube_dc4[1] = self.dc[0].ctypes.data, self.dc[1].ctypes.data
-        for i, f in enumerate(self.port_fields):
+        for i, g in enumerate(self.port_grids):
             p = d.port[i]
-            p.dims[0], p.dims[1], p.dims[2] = f.nx, f.ny, f.nz
-            p.h = f.h
-            p.rf4, p.ac4 = f.rf.ctypes.data, f.ac.ctypes.data
-            p.dc4 = self._port_dc[id(f)].ctypes.data
-            p.gate4 = f.dc[1].ctypes.data
+            p.dims[0], p.dims[1], p.dims[2] = g.nx, g.ny, g.nz
+            p.h = g.h
+            p.rf4, p.ac4, p.dc4, p.gate4 = g.rf.ctypes.data, g.ac.ctypes.data, g.dc.ctypes.data, g.gate.ctypes.data
             p.tone_khz = self.tones[i]
             p.v_ac = self.preset.v_ac
-        g0 = self.port_fields[0].geom
-        d.ch_axis_mm, d.ch_q1_start_mm = g0.axis(), g0.q1_start
+        d.ch_axis_mm, d.ch_q1_start_mm = self.port_grids[0].axis_mm, self.port_grids[0].q1_start_mm
         d.v_rf, d.f_rf, d.pressure_pa, d.temp_k, d.dt = (self.preset.v_rf, F_RF, self.preset.pressure_pa,
                                                          self.preset.temp_k, DT)
         d.gate_bias_v = GATE_BIAS_V
@@ -390,16 +435,17 @@ class TandemModel:
         except Exception:
             pass
 
-    def advance(self, steps: int) -> float:
-        """Advance every track by ``steps`` global steps (lib.rs:176-276); returns device ms."""
+    def advance(self, steps: int) -> "TandemStats":
+        """Advance every track by ``steps`` global steps (lib.rs:176-276)."""
         h = self._engine()
         t = self.tracks.native()
-        ms = C.c_double(0.0)
+        st = N.mq_tandem_stats()
         _check_t(N.lib().mq_tandem_advance(h, C.byref(t), self.tracks.n, C.c_uint64(self.step),
-                                           C.c_uint64(int(steps)), self.counts, C.byref(ms)), "mq_tandem_advance", h)
+                                           C.c_uint64(int(steps)), self.counts, C.byref(st)), "mq_tandem_advance", h)
         self.step += int(steps)
-        self.device_ms += ms.value
-        return ms.value
+        self.device_ms += st.kernel_ms
+        self.last_stats = TandemStats.from_native(st)
+        return self.last_stats
 
     def port_counts(self) -> list:
         return [PortCounts.from_native(c) for c in self.counts]

@@ -412,7 +412,7 @@ static void collide_(double v[3], uint64_t* rng, double nsd, double mr, double s
     for (int a = 0; a < 3; ++a) v[a] = v[a] - mr * gv[a] + mr * gl * nn[a];
 }
 
-static void run_track_(const tctx* C, size_t k, uint32_t* counts) {
+static void run_track_(const tctx* C, size_t k, uint32_t* counts, uint64_t* nsteps) {
     const mqt_desc* d = C->d;
     mqt_tracks* tr = C->tr;
     const int sp = tr->sp[k];
@@ -421,8 +421,13 @@ static void run_track_(const tctx* C, size_t k, uint32_t* counts) {
         if (reg >= LOST) return;
         const double* dr = C->drive + 10 * s;
         double x[3] = {tr->x[k], tr->y[k], tr->z[k]}, v[3] = {tr->vx[k], tr->vy[k], tr->vz[k]}, e[3];
-        if (reg == SPLIT || reg == COMBINE) cube_field_(d, d->cube_dc4[reg == COMBINE], x, dr[0], e);
-        else port_field_(&d->port[reg - 1], d->gate_bias_v, x, dr[0], dr[reg], e);
+        if (reg == SPLIT || reg == COMBINE) {
+            cube_field_(d, d->cube_dc4[reg == COMBINE], x, dr[0], e);
+            nsteps[0] += 1;
+        } else {
+            port_field_(&d->port[reg - 1], d->gate_bias_v, x, dr[0], dr[reg], e);
+            nsteps[d->port[reg - 1].tone_khz == 0.0 ? 2 : 1] += 1;
+        }
         for (int a = 0; a < 3; ++a) {   /* transport_step, lib.rs:90-103 */
             v[a] += C->qmdt[sp] * e[a];
             x[a] += v[a] * d->dt;
@@ -465,16 +470,17 @@ typedef struct {
     const tctx* C;
     size_t i0, i1;
     uint32_t counts[9 * MQT_NC];
+    uint64_t nsteps[3];
 } tjob;
 
 static void* tworker(void* arg) {
     tjob* j = (tjob*)arg;
-    for (size_t k = j->i0; k < j->i1; ++k) run_track_(j->C, k, j->counts);
+    for (size_t k = j->i0; k < j->i1; ++k) run_track_(j->C, k, j->counts, j->nsteps);
     return NULL;
 }
 
 int mqt_advance(const mqt_desc* d, mqt_tracks* tr, size_t n, uint64_t step0, uint64_t steps, uint32_t* counts,
-                int32_t threads) {
+                int32_t threads, uint64_t* nsteps) {
     if (d->nspecies < 1 || d->nspecies > 5) return -1;
     for (size_t k = 0; k < n; ++k)
         if (tr->sp[k] < 0 || tr->sp[k] >= d->nspecies || tr->region[k] < 0 || tr->region[k] > DETECTED ||
@@ -525,8 +531,11 @@ int mqt_advance(const mqt_desc* d, mqt_tracks* tr, size_t n, uint64_t step0, uin
     for (int t = 1; t < nt; ++t) pthread_create(&th[t], NULL, tworker, &jobs[t]);
     tworker(&jobs[0]);
     for (int t = 1; t < nt; ++t) pthread_join(th[t], NULL);
-    for (int t = 0; t < nt; ++t)
+    for (int t = 0; t < nt; ++t) {
         for (int q = 0; q < 9 * MQT_NC; ++q) counts[q] += jobs[t].counts[q];
+        if (nsteps)
+            for (int q = 0; q < 3; ++q) nsteps[q] += jobs[t].nsteps[q];
+    }
     free(jobs);
     free(th);
     free(drive);

@@ -81,9 +81,10 @@ int    mqt_inject(const mqt_desc* d, uint64_t seed, int mouth_start, mqt_tracks*
 void   mqt_enter(mqt_tracks* tr, size_t k, int port, int from_region, double seam, const double c[2], double axis,
                  uint32_t counts[MQT_NC]);
 void   mqt_leave(mqt_tracks* tr, size_t k, int port, double seam, const double c[2], double axis, uint32_t counts[MQT_NC]);
-/* global steps [step0, step0 + steps); counts[9 * MQT_NC] accumulate */
+/* global steps [step0, step0 + steps); counts[9 * MQT_NC] and nsteps[3] (executed track-steps:
+ * cube, driven port, idle port; may be NULL) accumulate */
 int    mqt_advance(const mqt_desc* d, mqt_tracks* tr, size_t n, uint64_t step0, uint64_t steps,
-                   uint32_t* counts, int32_t threads);
+                   uint32_t* counts, int32_t threads, uint64_t* nsteps);
 
 #ifdef __cplusplus
 }

@@ -78,7 +78,8 @@ def lib():
         L.mqt_enter.restype = None
         L.mqt_leave.argtypes = [P(Tracks), C.c_size_t, C.c_int, C.c_double, P(C.c_double), C.c_double, P(C.c_uint32)]
         L.mqt_leave.restype = None
-        L.mqt_advance.argtypes = [P(Desc), P(Tracks), C.c_size_t, C.c_uint64, C.c_uint64, P(C.c_uint32), C.c_int32]
+        L.mqt_advance.argtypes = [P(Desc), P(Tracks), C.c_size_t, C.c_uint64, C.c_uint64, P(C.c_uint32), C.c_int32,
+                                  P(C.c_uint64)]
         L.mqt_advance.restype = C.c_int
         _lib = L
     return _lib
@@ -153,12 +154,15 @@ def inject(d: Desc, seed: int, mouth_start: bool, n: int) -> State:
     return s
 
 
-def advance(d: Desc, s: State, step0: int, steps: int, counts: np.ndarray | None = None, threads: int = 0) -> np.ndarray:
-    """Advance in place; returns the (9, 21) uint32 counters (accumulated into ``counts``)."""
+def advance(d: Desc, s: State, step0: int, steps: int, counts: np.ndarray | None = None, threads: int = 0,
+            nsteps: np.ndarray | None = None) -> np.ndarray:
+    """Advance in place; returns the (9, 21) uint32 counters (accumulated into ``counts``);
+    ``nsteps`` (3 uint64: cube, driven port, idle port track-steps) accumulates if given."""
     cnt = np.zeros((9, NC), np.uint32) if counts is None else counts
     t = s.native()
+    ns = nsteps.ctypes.data_as(C.POINTER(C.c_uint64)) if nsteps is not None else None
     rc = lib().mqt_advance(C.byref(d), C.byref(t), s.n, C.c_uint64(step0), C.c_uint64(steps),
-                           cnt.ctypes.data_as(C.POINTER(C.c_uint32)), int(threads))
+                           cnt.ctypes.data_as(C.POINTER(C.c_uint32)), int(threads), ns)
     if rc != 0:
         raise ValueError(f"mqt_advance failed ({rc})")
     return cnt

@@ -78,3 +78,60 @@ def test_tandem_gpu_refuses_bad_tracks(tandem_small):
     m.tracks.region[5] = 0
     m.advance(10)   # the model is still usable
     m.close()
+
+
+def test_tandem_gpu_replica_grids_match_shared(tandem_small):
+    """Nine device-resident copies of one grid give exactly the shared-grid result."""
+    a = tandem_small(n=150, seed=5)
+    pg = a.port_grids[0]
+    b = tandem_small(n=150, seed=5, port_grids=[pg] + [pg.replica() for _ in range(8)])
+    for m in (a, b):
+        m.advance(6000)
+    _same_tracks(a.tracks, b.tracks)
+    assert np.array_equal(a.counts_array(), b.counts_array())
+    st = b.last_stats
+    assert st.track_steps == st.steps_cube + st.steps_port + st.steps_idle > 0
+    a.close()
+    b.close()
+
+
+def test_tandem_gpu_step_counts_match_oracle(tandem_small):
+    m = tandem_small(n=500, seed=8)
+    d = O.desc_from(m.desc)
+    ref = O.inject(d, 8, True, 500)
+    ns = np.zeros(3, np.uint64)
+    O.advance(d, ref, 0, 7000, nsteps=ns)
+    st = m.advance(7000)
+    assert (st.steps_cube, st.steps_port, st.steps_idle) == tuple(int(v) for v in ns)
+    assert st.launches >= 1 and st.kernel_ms > 0
+    m.close()
+
+
+def test_port_track_advances_like_the_fp64_channel_engine(tandem_small, s14_coarse):
+    """The GPU tandem's port region against the GPU FP64 channel engine over one 128-step block
+    (lib.rs:458-482): position within 1e-12 m, velocity within 1e-7 m/s, equal RNG state."""
+    from multiq_workbench_gb300 import tandem as T
+    m = tandem_small(n=1, seed=42)
+    f = s14_coarse
+    ph = mq.Physics.correct(m.preset.pressure_pa)
+    ph.dt, ph.t_max = T.DT, 3e-3
+    sp = m.preset.species[0]
+    job = mq.Job(mq.Species(sp.mass, sp.z, sp.ccs), mq.RfAc(m.preset.v_rf, T.F_RF, m.preset.v_ac, m.tones[0] * 1e3), 1, 42)
+    with mq.Engine(f, mq.PREC_F64) as eng:
+        eng.set_dc(list(T.DC_CAL))
+        ions = eng.inject([job], ph)
+        ions.ph_ac[0] = 0.0
+        ions.ph_rf[0] = 0.0
+        tr = m.tracks
+        tr.x[0], tr.y[0], tr.z[0] = ions.x[0], ions.y[0], ions.z[0]
+        tr.vx[0], tr.vy[0], tr.vz[0] = ions.vx[0], ions.vy[0], ions.vz[0]
+        tr.rng[0], tr.sp[0], tr.region[0], tr.last[0] = ions.rng[0], 0, 1, -1
+        eng.run_ions([job], ph, ions, max_more=128)
+    m.advance(128)
+    assert ions.status[0] == 0 and ions.steps[0] == 128 and tr.region[0] == 1
+    for a in ("x", "y", "z"):
+        assert abs(getattr(ions, a)[0] - getattr(tr, a)[0]) < 1e-12
+    for a in ("vx", "vy", "vz"):
+        assert abs(getattr(ions, a)[0] - getattr(tr, a)[0]) < 1e-7
+    assert int(ions.rng[0]) == int(tr.rng[0])
+    m.close()

@@ -213,3 +213,37 @@ def test_frame_census(tandem_small):
         c[0], c[1:10].sum(), c[10], c[11], c[12], c[13])
     assert f.points.shape == (int((m.tracks.region <= 10).sum()), 5)
     assert f.size_mm == pytest.approx(m.size * 1000.0)
+
+
+def test_port_track_advances_like_the_channel_integrator(tandem_small, s14_coarse):
+    """A track inside a driven port advances like the FP64 channel integrator (world.rs:498-536)
+    over one 128-step block: position within 1e-12 m, velocity within 1e-7 m/s, equal RNG state
+    (the reference's check, lib.rs:458-482).  Both sides are oracles; the drives differ only in
+    the rounding of the phase argument."""
+    from oracle import mqref as R
+    m = tandem_small(n=1, seed=42)
+    d = O.desc_from(m.desc)
+    f = s14_coarse
+    ph = mq.Physics.correct(m.preset.pressure_pa)
+    ph.dt, ph.t_max = T.DT, 3e-3
+    sp = m.preset.species[0]
+    job = mq.Job(mq.Species(sp.mass, sp.z, sp.ccs), mq.RfAc(m.preset.v_rf, T.F_RF, m.preset.v_ac, m.tones[0] * 1e3), 1, 42)
+    b = R.batch(ph, job.drive.v_rf, job.drive.f_rf, f.geom.axis(), f.geom.layers())
+    b.rf_phase0 = 1
+    ions = R.inject(b, [job], 1)
+    ions.ph_ac[0] = 0.0   # the reference's check sets the AC phase offset to 0 (sin 0, cos 1)
+    ions.ph_rf[0] = 0.0
+    tr = O.State(1)
+    tr.x[0], tr.y[0], tr.z[0] = ions.x[0], ions.y[0], ions.z[0]
+    tr.vx[0], tr.vy[0], tr.vz[0] = ions.vx[0], ions.vy[0], ions.vz[0]
+    tr.rng[0], tr.sp[0], tr.region[0], tr.last[0] = ions.rng[0], 0, 1, -1
+    g3 = R.Grid3(f.nx, f.ny, f.nz, f.h, f.rf, f.ac, f.dc_field(T.DC_CAL))
+    R.run(g3, b, [job], ions, threads=1, max_more=128)
+    cnt = O.advance(d, tr, 0, 128)
+    assert ions.status[0] == 0 and ions.steps[0] == 128
+    assert tr.region[0] == 1 and not cnt.any()
+    for a, c in (("x", "x"), ("y", "y"), ("z", "z")):
+        assert abs(getattr(ions, a)[0] - getattr(tr, c)[0]) < 1e-12
+    for a in ("vx", "vy", "vz"):
+        assert abs(getattr(ions, a)[0] - getattr(tr, a)[0]) < 1e-7
+    assert int(ions.rng[0]) == int(tr.rng[0])
