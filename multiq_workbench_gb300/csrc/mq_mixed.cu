@@ -53,6 +53,10 @@ __device__ __forceinline__ uint4 philox(uint32_t k0, uint32_t k1, uint32_t c0, u
 }
 __device__ __forceinline__ float unif(uint32_t x) { return (float)(x >> 8) * 0x1.0p-24f; }   // top 24 bits
 __device__ __forceinline__ float unif16(uint32_t x16) { return (float)x16 * 0x1.0p-16f; }      // a 16-bit field
+// sin / cos of a uniform angle 2 pi u - pi (u in [0, 1)): the hardware approximations are accurate to
+// about 2^-21 on [-pi, pi], far below the Monte Carlo noise of the draws they serve, and a uniform
+// angle shifted by pi is still uniform
+__device__ __forceinline__ void angle_sincos(float u, float* s, float* c) { __sincosf(fmaf(u, 6.28318531f, -3.14159265f), s, c); }
 
 // ---------------------------------------------------------------- FP32 turn-based sine
 // sin / cos Taylor polynomials on [-pi/4, pi/4] (coefficients (-1)^k/(2k+1)!, (-1)^k/(2k)!)
@@ -100,8 +104,8 @@ __device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& 
 
 // ---------------------------------------------------------------- cell cache
 // Interleaved node records: node q occupies float4 [3q] = {RF.xyz, conductor mask},
-// [3q+1] = {combined DC.xyz, 0}, [3q+2] = {AC.xyz, 0} (48 B), so the 8 corners of a cell are
-// 4 runs of 96 contiguous bytes.
+// [3q+1] = {combined DC.xyz, conductor bits of the cell based at q}, [3q+2] = {AC.xyz, 0}
+// (48 B), so the 8 corners of a cell are 4 runs of 96 contiguous bytes.
 struct Cell {
     float R[3][8], D[3][8], A[3][8];   // corner values per field and component, corner q = a + 2b + 4c
     int32_t ci, cj, ck;
@@ -124,7 +128,7 @@ __device__ __forceinline__ void load_cell(const float4* __restrict__ nodes, cons
         c.R[0][q] = r.x; c.R[1][q] = r.y; c.R[2][q] = r.z;
         c.D[0][q] = d.x; c.D[1][q] = d.y; c.D[2][q] = d.z;
         c.A[0][q] = a.x; c.A[1][q] = a.y; c.A[2][q] = a.z;
-        m |= (r.w > 0.5f ? 1u : 0u) << q;
+        if (q == 0) m = __float_as_uint(d.w);   // conductor bits of the cell's corners
     }
     c.ci = ci; c.cj = cj; c.ck = ck; c.mask = m;
 }
@@ -175,7 +179,7 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
     uint64_t Prf = 0, Pac = 0, Wac = 0;
     const uint64_t Wrf = ((uint64_t)B.w_rf_hi << 32) | B.w_rf_lo;
     // drive sines advanced by rotation each step and re-evaluated exactly from the
-    // fixed-point phases every 16 loop iterations (warp-uniform), so rounding cannot build up
+    // fixed-point phases every 4 loop iterations (warp-uniform), so rounding cannot build up
     float srf = 0.f, crf = 1.f, sac = 0.f, cac = 1.f, cw_ac = 1.f, sw_ac = 0.f;
     float kick = 0.f, v_ac = 0.f, cand_a = 0.f, cand_b = 0.f;
     uint32_t k0 = 0, k1 = 0;
@@ -229,12 +233,12 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
                     Prf = orf + (uint64_t)n * Wrf;
                     Pac = oac + (uint64_t)n * Wac;
                     // drive state as an uninterrupted run has it: exact at the last step that is
-                    // a multiple of 16, then rotated forward (so re-queued ions continue bitwise)
+                    // a multiple of 4, then rotated forward (so re-queued ions continue bitwise)
                     {
-                        const uint32_t r16 = n & 15u;
-                        turn_sincos(Prf - (uint64_t)r16 * Wrf, srf, crf);
-                        turn_sincos(Pac - (uint64_t)r16 * Wac, sac, cac);
-                        for (uint32_t q = 0; q < r16; ++q) { rotate(srf, crf, B.cw_rf, B.sw_rf); rotate(sac, cac, cw_ac, sw_ac); }
+                        const uint32_t r4 = n & 3u;
+                        turn_sincos(Prf - (uint64_t)r4 * Wrf, srf, crf);
+                        turn_sincos(Pac - (uint64_t)r4 * Wac, sac, cac);
+                        for (uint32_t q = 0; q < r4; ++q) { rotate(srf, crf, B.cw_rf, B.sw_rf); rotate(sac, cac, cw_ac, sw_ac); }
                     }
                     const uint64_t key = io.rng[id];
                     k0 = (uint32_t)key; k1 = (uint32_t)(key >> 32);
@@ -252,13 +256,13 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
 
         bool append = false;
         // A lane steps its ion only when the ion's step count is congruent to the warp's
-        // iteration counter mod 16 (a freshly loaded ion waits at most 15 iterations).  Every
-        // warp-uniform event below (Philox refresh each 4 iterations, exact drive re-sync
-        // each 16) then falls on the same steps of every ion, whatever the scheduling, so
-        // per-ion results are reproducible bit for bit.
-        const bool act = have && (((iter ^ n) & 15u) == 0u);
+        // iteration counter mod 4 (a freshly loaded ion waits at most 3 iterations).  Every
+        // warp-uniform event below (Philox refresh and exact drive re-sync, each 4 iterations)
+        // then falls on the same steps of every ion, whatever the scheduling, so per-ion
+        // results are reproducible bit for bit.
+        const bool act = have && (((iter ^ n) & 3u) == 0u);
         if (!LEGACY && (iter & 3u) == 0u && act) rn = philox(k0, k1, (n >> 2) + 1u, 0u, 0u, 0u);
-        if ((iter & 15u) == 0u && act) { turn_sincos(Prf, srf, crf); turn_sincos(Pac, sac, cac); }
+        if ((iter & 3u) == 0u && act) { turn_sincos(Prf, srf, crf); turn_sincos(Pac, sac, cac); }
         ++iter;
         if (act) {
             // ---- field at the current position
@@ -293,8 +297,11 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
             // ---- collisions
             if (!LEGACY) {
                 const float u0 = unif((nprev & 3) == 0 ? rc.x : (nprev & 3) == 1 ? rc.y : (nprev & 3) == 2 ? rc.z : rc.w);
-                const float um = sqrtf(fmaf(uh[0], uh[0], fmaf(uh[1], uh[1], uh[2] * uh[2])));
-                if (u0 < fmaf(cand_a, um, cand_b)) {
+                // candidate if u0 < cand_a |u| + cand_b, tested on squares (no square root per step)
+                const float um2 = fmaf(uh[0], uh[0], fmaf(uh[1], uh[1], uh[2] * uh[2]));
+                const float du = u0 - cand_b;
+                if (du < 0.0f || du * du < cand_a * cand_a * um2) {
+                    const float um = sqrtf(um2);
                     const MixJob J = jobs[jid];
                     // one Philox block (128 bits) per candidate: two 24-bit uniforms for the
                     // Box-Muller radii, and five 16-bit uniforms (two Box-Muller angles, the
@@ -303,11 +310,11 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
                     const float u2v = B.u2v_f;
                     float v[3] = {uh[0] * u2v, uh[1] * u2v, uh[2] * u2v};
                     const float bound = fmaf(um, u2v, 6.0f * J.s_gas);
-                    const float g1 = sqrtf(-2.0f * logf(fmaxf(unif(r0.x), 0x1.0p-25f)));
-                    const float g2 = sqrtf(-2.0f * logf(fmaxf(unif(r0.y), 0x1.0p-25f)));
-                    float s1, c1;
-                    sincospif(2.0f * unif16(r0.z >> 16), &s1, &c1);
-                    const float c2 = cospif(2.0f * unif16(r0.z & 0xffffu));
+                    const float g1 = sqrtf(-2.0f * __logf(fmaxf(unif(r0.x), 0x1.0p-25f)));
+                    const float g2 = sqrtf(-2.0f * __logf(fmaxf(unif(r0.y), 0x1.0p-25f)));
+                    float s1, c1, s2, c2;
+                    angle_sincos(unif16(r0.z >> 16), &s1, &c1);
+                    angle_sincos(unif16(r0.z & 0xffffu), &s2, &c2);
                     float gv[3];
                     gv[0] = fmaf(-J.s_gas, g1 * c1, v[0]);
                     gv[1] = fmaf(-J.s_gas, g1 * s1, v[1]);
@@ -316,7 +323,7 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
                     if (unif16(r0.w >> 16) * bound < gl) {
                         const float cth = 2.0f * unif16(r0.w & 0xffffu) - 1.0f;
                         float sp, cp;
-                        sincospif(2.0f * unif16(((r0.x & 0xffu) << 8) | (r0.y & 0xffu)), &sp, &cp);
+                        angle_sincos(unif16(((r0.x & 0xffu) << 8) | (r0.y & 0xffu)), &sp, &cp);
                         const float sn = sqrtf(fmaxf(0.0f, 1.0f - cth * cth));
                         const float nn[3] = {sn * cp, sn * sp, cth};
                         const float v2u = B.v2u_f;
@@ -340,7 +347,7 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
                     if (vm > J.floor_v) {
                         const float cth = 2.0f * unif(r0.x) - 1.0f;
                         float sp, cp;
-                        sincospif(2.0f * unif(r0.y), &sp, &cp);
+                        angle_sincos(unif(r0.y), &sp, &cp);
                         const float sn = sqrtf(fmaxf(0.0f, 1.0f - cth * cth));
                         const float dd[3] = {sn * cp, sn * sp, cth};
                         const float v2u = B.v2u_f;
@@ -351,7 +358,7 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
                         }
                         ncoll += 1;
                     }
-                    const float mfp = -logf(fmaxf(unif(r0.z), 1e-7f)) * J.mfp_mean;
+                    const float mfp = -__logf(fmaxf(unif(r0.z), 1e-7f)) * J.mfp_mean;
                     const float vn = sqrtf(fmaf(v[0], v[0], fmaf(v[1], v[1], v[2] * v[2])));
                     const float st = floorf(mfp / fmaxf(vn, 1e-3f) / B.dt_f);
                     leg = st < 1.0f ? 1 : (st < 2147483520.0f ? (int32_t)st : 2147483647);
@@ -422,13 +429,23 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
     if (lane == 0 && steps_total) atomicAdd(&ctr->steps, steps_total);
 }
 
-// interleave RF | combined DC | AC into 48-byte node records (once per DC configuration)
+// interleave RF | combined DC | AC into 48-byte node records (once per DC configuration); the
+// spare w of the DC record holds the conductor bits of the 8 corners of the cell whose lowest
+// corner is this node (bit a + 2b + 4c), so a cell reload reads its crash mask in one word
 __global__ void k_pack_nodes(const float4* __restrict__ rf, const float4* __restrict__ dc, const float4* __restrict__ ac,
-                             float4* __restrict__ nodes, size_t n) {
+                             float4* __restrict__ nodes, size_t n, int32_t nx, int32_t ny, int32_t nz) {
     const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= n) return;
     nodes[3 * q] = rf[q];
-    nodes[3 * q + 1] = dc[q];
+    float4 d = dc[q];
+    const size_t sy = (size_t)nx, sz = (size_t)nx * (size_t)ny;
+    const int32_t i = (int32_t)(q % sy), j = (int32_t)((q / sy) % (size_t)ny), k = (int32_t)(q / sz);
+    uint32_t m = 0;
+    if (i < nx - 1 && j < ny - 1 && k < nz - 1)
+        for (int c = 0; c < 8; ++c)
+            m |= (rf[q + (size_t)(c & 1) + ((c & 2) ? sy : 0) + ((c & 4) ? sz : 0)].w > 0.5f ? 1u : 0u) << c;
+    d.w = __uint_as_float(m);
+    nodes[3 * q + 1] = d;
     nodes[3 * q + 2] = ac[q];
 }
 
@@ -576,7 +593,7 @@ cudaError_t pack_nodes(Scratch& s, DevGrid g, uint64_t grid_gen, cudaStream_t st
         if ((e = cudaMalloc(&s.nodes, bytes)) != cudaSuccess) return e;
         s.nodes_cap = bytes;
     }
-    k_pack_nodes<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(g.rf, g.dc, g.ac, static_cast<float4*>(s.nodes), n);
+    k_pack_nodes<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(g.rf, g.dc, g.ac, static_cast<float4*>(s.nodes), n, g.nx, g.ny, g.nz);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     *kernels += 1;
     s.nodes_gen = grid_gen;
