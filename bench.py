@@ -144,6 +144,25 @@ def cpu_rate(jobs, ph, dc, f, sample_jobs: int, threads: int, target_s: float | 
     return {"value": steps / dt, "steps": steps, "seconds": dt, "ions": n, "jobs": nj}
 
 
+def reduce_over_ranks(times, counts, device) -> tuple[list, list]:
+    """Whole-job figures of replicas: the slowest rank's times and the sum of every rank's
+    counts (one all-reduce each; a no-op without an initialised process group)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return [float(t) for t in times], [float(c) for c in counts]
+    tt = torch.tensor([float(t) for t in times], dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    cc = torch.tensor([float(c) for c in counts], dtype=torch.float64, device=device)
+    dist.all_reduce(cc, op=dist.ReduceOp.SUM)
+    return tt.tolist(), cc.tolist()
+
+
+def rank_seed0(rank: int) -> int:
+    """First job seed of a rank's replica of the workload (disjoint seed ranges per rank)."""
+    return rank * 1_000_003
+
+
 def flush_l2(buf):
     buf.fill_(1)
 
@@ -184,7 +203,7 @@ TANDEM_UNIT = "track-steps/s"
 TANDEM_BYTES = {"cube": 8 * 16 * 2, "port": 8 * 16 * 3, "idle": 8 * 16 * 4}
 
 
-def tandem_setup(args):
+def tandem_setup(args, rank: int = 0):
     """The tandem workload: Fig. 5 drives (tones 39 / 47 / 53 / 59.25 kHz on four ports, five
     idle ports gated +4 V), ubiquitin 6+..10+ mixture, tracks launched at the nine mouths, cube at
     0.51875 mm, the nine ports on the calibrated S14 channel grid at ``--port-h`` mm, each port
@@ -194,7 +213,8 @@ def tandem_setup(args):
     ch = mq.Fields.build(mq.Geom.s14(h_mm=h, n_xy=int(round(16.0 / h))))
     pg = mq.PortGrid.from_fields(ch)
     grids = [pg] * 9 if args.tandem_shared else [pg] + [pg.replica() for _ in range(8)]
-    m = mq.TandemModel(mq.DEFAULT_TONES, n=args.tracks, seed=486, fine=True, mouth_start=True, port_grids=grids)
+    m = mq.TandemModel(mq.DEFAULT_TONES, n=args.tracks, seed=486 + rank_seed0(rank), fine=True, mouth_start=True,
+                       port_grids=grids)
     wl = (f"tandem: {args.tracks:,} tracks at the nine mouths, Fig. 5 tones, ubiquitin 6+..10+, cube 0.51875 mm "
           f"{'x'.join(map(str, m.cube.dims))}, ports on S14 {h:g} mm {ch.nx}x{ch.ny}x{ch.nz} "
           f"({'one shared grid' if args.tandem_shared else 'nine device-resident copies'}), "
@@ -258,7 +278,7 @@ def run_tandem(args, rank: int, world: int):
     ge.build()
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
-    m, wl = tandem_setup(args)
+    m, wl = tandem_setup(args, rank)
     m.device = local
     pulse = m.tracks.copy()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
@@ -288,14 +308,8 @@ def run_tandem(args, rank: int, world: int):
     ts = sum(s.track_steps for s in sts)
     t_dev = sum(s.kernel_ms for s in sts) * 1e-3
     t_wall = sum(walls)
-    ts_all = float(ts)
-    if world > 1:   # replicas: every rank runs its own pulse; whole-job rate over the slowest rank
-        import torch.distributed as dist
-        tt = torch.tensor([t_dev, t_wall], dtype=torch.float64, device=f"cuda:{local}")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        sv = torch.tensor([ts_all], dtype=torch.float64, device=f"cuda:{local}")
-        dist.all_reduce(sv, op=dist.ReduceOp.SUM)
-        t_dev, t_wall, ts_all = float(tt[0]), float(tt[1]), float(sv[0])
+    # replicas: every rank runs its own pulse; whole-job rate over the slowest rank
+    (t_dev, t_wall), (ts_all,) = reduce_over_ranks([t_dev, t_wall], [ts], f"cuda:{local}")
     value = ts_all / t_dev
     e2e = ts_all / t_wall
     if rank != 0:
@@ -381,7 +395,7 @@ def main():
 
     ge.build()
     torch.cuda.set_device(local)
-    jobs, ph, dc = workload(ions_per_job=args.ions_per_job, seed0=rank * 1_000_003)
+    jobs, ph, dc = workload(ions_per_job=args.ions_per_job, seed0=rank_seed0(rank))
     f = fields()
     eng = mq.Engine(f, mq.PREC_MIXED, device=local)
     tuned = None
@@ -418,14 +432,7 @@ def main():
     clk = clocks.stop()
     t_dev = sum(dev_ms) * 1e-3
     t_wall = sum(walls)
-    if dist:
-        tt = torch.tensor([t_dev, t_wall], dtype=torch.float64, device=f"cuda:{local}")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        st = torch.tensor([float(steps_total)], dtype=torch.float64, device=f"cuda:{local}")
-        dist.all_reduce(st, op=dist.ReduceOp.SUM)
-        t_dev, t_wall, steps_all = float(tt[0]), float(tt[1]), float(st[0])
-    else:
-        steps_all = float(steps_total)
+    (t_dev, t_wall), (steps_all,) = reduce_over_ranks([t_dev, t_wall], [steps_total], f"cuda:{local}")
     value = steps_all / t_dev
     e2e_value = steps_all / t_wall
     counts = {k: int(sum(getattr(o, k) for o in out)) for k in ("transmitted", "returned", "crashed", "left", "timeout")}
@@ -462,8 +469,8 @@ def main():
     hbm = hbm or 6800.0
     kern_s = sum(step_ms) * 1e-3
     achieved = BYTES_PER_ION_STEP * steps_total / kern_s / 1e9
-    # DRAM bytes of one k_mixed launch from the committed ncu summary of this workload
-    prof = ROOT / "profiles" / "k_mixed_batched_sweep.md"
+    # DRAM bytes of one full-size k_mixed launch from the committed one-pass ncu summary
+    prof = ROOT / "profiles" / "k_mixed_batched_sweep_full.md"
     traffic = None
     if prof.exists():
         import re
