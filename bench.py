@@ -197,34 +197,38 @@ def run_reference(args, rank: int, world: int):
     print(json.dumps(line), flush=True)
 
 
-TANDEM_METRIC = "track-steps/s, 1 GB300: nine-channel tandem transport (FP64 kernel, bit-exact with the CPU oracle)"
+TANDEM_METRIC = "track-steps/s, 1 GB300: nine-channel tandem transport, mixed precision vs plain FP64 at matched counts"
 TANDEM_UNIT = "track-steps/s"
 # algorithmic bytes per track-step: 8 corner nodes x float4 (16 B) x the fields the region reads
-TANDEM_BYTES = {"cube": 8 * 16 * 2, "port": 8 * 16 * 3, "idle": 8 * 16 * 4}
+# (the mixed engine folds the gate bias of idle ports into their DC records)
+TANDEM_BYTES = {"f64": {"cube": 8 * 16 * 2, "port": 8 * 16 * 3, "idle": 8 * 16 * 4},
+                "mixed": {"cube": 8 * 16 * 2, "port": 8 * 16 * 3, "idle": 8 * 16 * 3}}
 
 
-def tandem_setup(args, rank: int = 0):
+def tandem_setup(args, rank: int = 0, precision: int = 1, grids=None):
     """The tandem workload: Fig. 5 drives (tones 39 / 47 / 53 / 59.25 kHz on four ports, five
     idle ports gated +4 V), ubiquitin 6+..10+ mixture, tracks launched at the nine mouths, cube at
     0.51875 mm, the nine ports on the calibrated S14 channel grid at ``--port-h`` mm, each port
     holding its own device-resident copy of that grid unless ``--tandem-shared``."""
     import multiq_workbench_gb300 as mq
     h = float(args.port_h)
-    ch = mq.Fields.build(mq.Geom.s14(h_mm=h, n_xy=int(round(16.0 / h))))
-    pg = mq.PortGrid.from_fields(ch)
-    grids = [pg] * 9 if args.tandem_shared else [pg] + [pg.replica() for _ in range(8)]
+    if grids is None:
+        ch = mq.Fields.build(mq.Geom.s14(h_mm=h, n_xy=int(round(16.0 / h))))
+        pg = mq.PortGrid.from_fields(ch)
+        grids = [pg] * 9 if args.tandem_shared else [pg] + [pg.replica() for _ in range(8)]
     m = mq.TandemModel(mq.DEFAULT_TONES, n=args.tracks, seed=486 + rank_seed0(rank), fine=True, mouth_start=True,
-                       port_grids=grids)
+                       port_grids=grids, precision=precision)
+    g0 = grids[0]
     wl = (f"tandem: {args.tracks:,} tracks at the nine mouths, Fig. 5 tones, ubiquitin 6+..10+, cube 0.51875 mm "
-          f"{'x'.join(map(str, m.cube.dims))}, ports on S14 {h:g} mm {ch.nx}x{ch.ny}x{ch.nz} "
+          f"{'x'.join(map(str, m.cube.dims))}, ports on S14 {h:g} mm {g0.nx}x{g0.ny}x{g0.nz} "
           f"({'one shared grid' if args.tandem_shared else 'nine device-resident copies'}), "
           f"{args.tandem_steps} global steps per bench step")
     return m, wl
 
 
-def tandem_bytes(st) -> float:
-    return (TANDEM_BYTES["cube"] * st.steps_cube + TANDEM_BYTES["port"] * st.steps_port
-            + TANDEM_BYTES["idle"] * st.steps_idle)
+def tandem_bytes(st, kind: str = "mixed") -> float:
+    b = TANDEM_BYTES[kind]
+    return b["cube"] * st.steps_cube + b["port"] * st.steps_port + b["idle"] * st.steps_idle
 
 
 def tandem_cpu(m, pulse, steps: int, target_s: float, threads: int) -> dict:
@@ -278,17 +282,17 @@ def run_tandem(args, rank: int, world: int):
     ge.build()
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
-    m, wl = tandem_setup(args, rank)
+    m, wl = tandem_setup(args, rank, mq.PREC_MIXED)
     m.device = local
     pulse = m.tracks.copy()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
 
-    def one():
-        m.tracks = pulse.copy()
-        m.step = 0
-        m.counts = type(m.counts)()
+    def one(model=m):
+        model.tracks = pulse.copy()
+        model.step = 0
+        model.counts = type(model.counts)()
         t0 = time.perf_counter()
-        st = m.advance(args.tandem_steps)
+        st = model.advance(args.tandem_steps)
         return st, time.perf_counter() - t0
 
     for _ in range(args.warmup):
@@ -320,6 +324,27 @@ def run_tandem(args, rank: int, world: int):
     achieved = sum(tandem_bytes(s) for s in sts) / (sum(s.kernel_ms for s in sts) * 1e-3) / 1e9
     f = m.frame()
     cnt = m.counts_array()
+    extra = {}
+    if not args.no_f64:
+        # the FP64 kernel (bit-exact with the oracle) on the same pulse: speed and matched counts
+        m64, _ = tandem_setup(args, rank, mq.PREC_F64, grids=m.port_grids)
+        m64.device = local
+        s64, _ = one(m64)
+        c64 = m64.counts_array()
+        f64 = m64.frame()
+        m64.close()
+
+        def pull(a, b):
+            return (a - b) / math.sqrt(max(a + b, 1))
+        cmp = {}
+        for name, a, b in (("entered", cnt[:, 0].sum(), c64[:, 0].sum()), ("returned", cnt[:, 1].sum(), c64[:, 1].sum()),
+                           ("lost_in_ports", cnt[:, 15].sum(), c64[:, 15].sum()), ("split", f.split, f64.split),
+                           ("channel", f.channel, f64.channel), ("lost", f.lost, f64.lost)):
+            cmp[name] = {"mixed": int(a), "fp64": int(b), "pull": pull(float(a), float(b))}
+        extra["fp64_gpu"] = {"value": s64.track_steps / (s64.kernel_ms * 1e-3), "unit": TANDEM_UNIT,
+                             "speedup_mixed_over_fp64": (ts / t_dev) / (s64.track_steps / (s64.kernel_ms * 1e-3)),
+                             "roofline_achieved_gbs": tandem_bytes(s64, "f64") / (s64.kernel_ms * 1e-3) / 1e9,
+                             "sample": "the same pulse and steps", "counts": cmp}
     cpu = None
     if not args.no_cpu:
         r = tandem_cpu(m, pulse, args.tandem_steps, 12.0, threads)
@@ -328,7 +353,7 @@ def run_tandem(args, rank: int, world: int):
     last = sts[-1]
     line = {"metric": TANDEM_METRIC, "value": value, "unit": TANDEM_UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
             "config": {"workload": wl, "tracks": args.tracks, "global_steps": args.tandem_steps,
                        "l2_flush": "256 MB write before every timed step"},
             "track_steps_per_step": ts / args.steps,
@@ -337,7 +362,7 @@ def run_tandem(args, rank: int, world: int):
             "gpu_launches": int(sum(s.launches for s in sts)),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                          "traffic": None, "peak_source": "measured hbm_gbs" if peaks.get("hbm_gbs") else "fallback",
-                         "kernel": "k_tandem", "algorithmic_bytes_per_track_step": TANDEM_BYTES},
+                         "kernel": "k_tm_step", "algorithmic_bytes_per_track_step": TANDEM_BYTES["mixed"]},
             "cpu_baseline": cpu, "clocks": clk,
             "census": {"split": f.split, "channel": f.channel, "combine": f.combine, "lost": f.lost, "back": f.back,
                        "detected": f.detected},
@@ -345,6 +370,7 @@ def run_tandem(args, rank: int, world: int):
                       "revisits": int(cnt[:, 3].sum()), "from_other": int(cnt[:, 4].sum()),
                       "retry_matrix": cnt[:, 5:14].tolist(), "reverse_entries": int(cnt[:, 14].sum()),
                       "lost": cnt[:, 15].tolist(), "by_charge": cnt[:, 16:21].sum(0).tolist()}}
+    line.update(extra)
     print(json.dumps(line), flush=True)
     m.close()
 

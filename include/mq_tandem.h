@@ -18,7 +18,7 @@
 #ifndef MQ_TANDEM_H
 #define MQ_TANDEM_H
 
-#include "mq_grid.h"
+#include "mq_engine.h"
 
 #ifdef __cplusplus
 extern "C" {
@@ -99,7 +99,10 @@ typedef struct mq_tandem_desc {
     double ch_axis_mm, ch_q1_start_mm; /* channel axis (x = y) and Q1 start, shared geometry */
     double v_rf, f_rf, pressure_pa, temp_k, dt;
     double gate_bias_v;                /* 4 V in the reference                                */
-    int32_t nspecies, pad2;
+    int32_t nspecies;
+    int32_t precision;                 /* MQ_PREC_F64: bit-exact FP64 twin of Model::advance;
+                                          MQ_PREC_MIXED: FP32 fields, compensated FP32 state,
+                                          Philox thermal collisions (statistically equivalent) */
     mq_tandem_species species[8];      /* nspecies <= 5: five charge-state counters per port */
 } mq_tandem_desc;
 
@@ -132,7 +135,8 @@ typedef struct mq_tandem_stats {
 } mq_tandem_stats;
 
 /* advance tracks (host arrays, in place) by `steps` global steps starting at global step
- * step0; counts[9] accumulate; stats may be NULL.  Synchronous. */
+ * step0; counts[9] accumulate; stats may be NULL.  Synchronous.  With MQ_PREC_MIXED the
+ * track's rng word is the key of its counter-based generator and is left unchanged. */
 mq_status mq_tandem_advance(mq_tandem* t, mq_tracks* tr, size_t n, uint64_t step0, uint64_t steps,
                             mq_port_counts counts[9], mq_tandem_stats* stats);
 mq_status mq_tandem_frame(const mq_tracks* tr, size_t n, mq_tandem_frame_counts* out);

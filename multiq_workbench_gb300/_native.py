@@ -13,6 +13,8 @@ _LIB_PATH = Path(__file__).resolve().parent / "libmqgb.so"
 _lib = None
 
 MQ_OK = 0
+MQ_PREC_F64 = 0     # include/mq_engine.h
+MQ_PREC_MIXED = 1
 MQ_ERRORS = {
     -1: "invalid argument",
     -2: "CUDA runtime error",
@@ -129,7 +131,7 @@ class mq_tandem_desc(C.Structure):
                 ("cube_dc4", C.c_void_p * 2), ("port", mq_tandem_port * 9), ("ch_axis_mm", C.c_double),
                 ("ch_q1_start_mm", C.c_double), ("v_rf", C.c_double), ("f_rf", C.c_double),
                 ("pressure_pa", C.c_double), ("temp_k", C.c_double), ("dt", C.c_double), ("gate_bias_v", C.c_double),
-                ("nspecies", C.c_int32), ("pad2", C.c_int32), ("species", mq_tandem_species * 8)]
+                ("nspecies", C.c_int32), ("precision", C.c_int32), ("species", mq_tandem_species * 8)]
 
 
 class mq_tracks(C.Structure):

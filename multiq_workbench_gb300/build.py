@@ -29,6 +29,7 @@ CUDA_UNITS = [
     ("mq_f64.cu", ["--fmad=false"]),
     ("mq_mixed.cu", []),
     ("mq_tandem.cu", ["--fmad=false"]),
+    ("mq_tandem_mixed.cu", []),
     ("mq_noalloc.cu", []),
 ]
 CXX_UNITS = ["mq_grid.cpp", "mq_engine.cpp", "mq_cube.cpp"]

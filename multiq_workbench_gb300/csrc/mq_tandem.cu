@@ -14,6 +14,7 @@
 #include "mq_cube_geom.h"
 #include "mq_phys.h"
 #include "mq_tandem.h"
+#include "mq_tandem_internal.h"
 
 namespace {
 
@@ -270,6 +271,7 @@ struct mq_tandem {
     size_t drive_cap = 0;
     uint32_t* counts = nullptr;
     unsigned long long* stepc = nullptr;   // executed track-steps: cube, driven port, idle port
+    mqtm::State* mix = nullptr;            // the mixed-precision engine (MQ_PREC_MIXED)
     cudaStream_t st = nullptr;
     cudaEvent_t ev[2] = {nullptr, nullptr};
 };
@@ -304,7 +306,8 @@ mq_status mq_tandem_create(const mq_tandem_desc* d, int32_t device, mq_tandem** 
     if (!out) return MQ_ERR_INVALID;
     *out = nullptr;
     if (!d || !d->cube_rf4 || !d->cube_dc4[0] || !d->cube_dc4[1] || d->nspecies < 1 ||
-        d->nspecies > 5 || !(d->dt > 0) || !(d->cube_h_mm > 0))   // five charge-state counters per port
+        d->nspecies > 5 || !(d->dt > 0) || !(d->cube_h_mm > 0) ||   // five charge-state counters per port
+        (d->precision != MQ_PREC_F64 && d->precision != MQ_PREC_MIXED))
         return MQ_ERR_INVALID;
     for (int a = 0; a < 3; ++a)
         if (d->cube_dims[a] < 2) return MQ_ERR_INVALID;
@@ -379,6 +382,19 @@ mq_status mq_tandem_create(const mq_tandem_desc* d, int32_t device, mq_tandem** 
         C.sp[s].mr = mg / (m + mg);
         C.sp[s].nsd = (ngas * (d->species[s].ccs * 1e-20)) * d->dt;
     }
+    if (d->precision == MQ_PREC_MIXED) {
+        mqtm::DevFields f;
+        f.crf = C.crf;
+        f.cdc[0] = C.cdc[0];
+        f.cdc[1] = C.cdc[1];
+        for (int i = 0; i < 9; ++i) {
+            f.prf[i] = C.port[i].rf; f.pac[i] = C.port[i].ac; f.pdc[i] = C.port[i].dc; f.pgate[i] = C.port[i].gate;
+        }
+        std::string err;
+        t->mix = mqtm::create(*d, f, t->st, err);
+        if (!t->mix) { mq_tandem_destroy(t); return MQ_ERR_NOMEM; }
+        if (cudaStreamSynchronize(t->st) != cudaSuccess) return bail(MQ_ERR_CUDA);
+    }
     *out = t;
     return MQ_OK;
 }
@@ -392,6 +408,7 @@ void mq_tandem_destroy(mq_tandem* t) {
     if (t->drive) cudaFree(t->drive);
     if (t->counts) cudaFree(t->counts);
     if (t->stepc) cudaFree(t->stepc);
+    if (t->mix) mqtm::destroy(t->mix);
     for (auto& e : t->ev) if (e) cudaEventDestroy(e);
     if (t->st) cudaStreamDestroy(t->st);
     delete t;
@@ -425,6 +442,7 @@ mq_status mq_tandem_advance(mq_tandem* t, mq_tracks* tr, size_t n, uint64_t step
     T.x = (double*)dev[0]; T.y = (double*)dev[1]; T.z = (double*)dev[2];
     T.vx = (double*)dev[3]; T.vy = (double*)dev[4]; T.vz = (double*)dev[5];
     T.rng = (uint64_t*)dev[6]; T.sp = (int32_t*)dev[7]; T.region = (int32_t*)dev[8]; T.last = (int32_t*)dev[9];
+    const mqtm::Tracks64 T64{T.x, T.y, T.z, T.vx, T.vy, T.vz, T.rng, T.sp, T.region, T.last};
     for (size_t i = 0; i < n; ++i)   // the kernel indexes species constants and counters by these
         if (tr->sp[i] < 0 || tr->sp[i] >= t->desc.nspecies || tr->region[i] < 0 || tr->region[i] > R_DETECTED ||
             tr->last[i] < -1 || tr->last[i] > 8)
@@ -455,8 +473,16 @@ mq_status mq_tandem_advance(mq_tandem* t, mq_tracks* tr, size_t n, uint64_t step
         // pageable source: the call returns once the host buffer has been staged, so it may be refilled next
         if (k) TCK(cudaMemcpyAsync(t->drive, dtab.data(), k * 10 * 8, cudaMemcpyHostToDevice, t->st), "drive upload");
         h2d += k * 10 * 8;
-        if (s == 0) TCK(cudaEventRecord(t->ev[0], t->st), "event");   // times the kernels (and later table blocks)
+        if (s == 0) {
+            TCK(cudaEventRecord(t->ev[0], t->st), "event");   // times the kernels (and later table blocks)
+            if (t->mix) TCK(mqtm::load(t->mix, T64, (uint32_t)n, t->st, &launches), "mixed tandem load");
+        }
         if (!steps) break;
+        if (t->mix) {
+            TCK(mqtm::run(t->mix, (uint32_t)n, (const double*)t->drive, step0 + s, k, t->counts, t->stepc, t->st, &launches),
+                "mixed tandem kernel");
+            continue;
+        }
         for (uint64_t q = 0; q < k && n; q += per, ++launches) {
             const uint64_t m = k - q < per ? k - q : per;
             k_tandem<<<(unsigned)((n + 127) / 128), 128, 0, t->st>>>(t->C, T, (uint32_t)n, (const double*)t->drive + q * 10,
@@ -464,6 +490,7 @@ mq_status mq_tandem_advance(mq_tandem* t, mq_tracks* tr, size_t n, uint64_t step
             TCK(cudaGetLastError(), "tandem kernel");
         }
     }
+    if (t->mix) TCK(mqtm::store(t->mix, T64, (uint32_t)n, t->st, &launches), "mixed tandem store");
     TCK(cudaEventRecord(t->ev[1], t->st), "event");
     for (int k = 0; k < 10; ++k) TCK(cudaMemcpyAsync(host[k], dev[k], sz[k] * n, cudaMemcpyDeviceToHost, t->st), "track download");
     TCK(cudaMemcpyAsync(cnt.data(), t->counts, cnt.size() * 4, cudaMemcpyDeviceToHost, t->st), "counter download");

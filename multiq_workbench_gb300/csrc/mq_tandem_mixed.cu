@@ -1,0 +1,719 @@
+// Mixed-precision tandem engine for sm_103a: the nine-channel transport of
+// trapsim::Model::advance (simulation/trapsim/src/lib.rs:176-385) with the batched engine's
+// arithmetic (FP32 fields and kinematics, compensated FP32 position and velocity).
+//
+//   * every launch advances all live tracks by one chunk of global steps; a bucket pass first
+//     groups the tracks by region (splitter, nine ports, combiner), so warps start out
+//     reading one field grid (ragged batching by field id) and lost / finished tracks drop out;
+//   * position and velocity are FP32 double-floats in grid units of the track's current region
+//     (cube grid in mm, or the port's grid); region changes convert through FP64 with
+//     trapsim's enter / leave arithmetic (lib.rs:338-385);
+//   * fields as interleaved node records: cube {RF, region DC} 32 B, port {RF, DC (+ gate
+//     bias on idle ports), AC} 48 B with the cell's conductor bits in a spare word;
+//   * drive values per global step read (as FP32) from the FP64 engine's drive table; thermal
+//     collisions with Philox-4x32-10 keyed by the track key and the global step (all lanes
+//     share the global step, so the generator runs warp-uniformly);
+//   * cube losses by the geometry test in FP32, skipped in the interior box where every
+//     face is farther than the post tops (geometry.rs:166 makes such points free).
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "mq_cube_geom.h"
+#include "mq_phys.h"
+#include "mq_tandem_internal.h"
+
+namespace mqtm {
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+constexpr int R_SPLIT = 0, R_COMBINE = 10, R_LOST = 11;
+constexpr int kNC = 21;        // counters per port
+constexpr int kBuckets = 11;   // live regions 0..10
+constexpr double Z_EXIT = 18.6e-3, Z_RETURN = 0.5e-3;   // world.rs:21-22
+constexpr uint32_t kChunk = 256;                        // global steps per launch
+
+// ---------------------------------------------------------------- Philox-4x32-10
+// Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy as 1, 2, 3" (SC'11).
+__device__ __forceinline__ uint4 philox(uint32_t k0, uint32_t k1, uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        if (r) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
+        const uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
+        const uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
+        const uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+        c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+    }
+    return make_uint4(c0, c1, c2, c3);
+}
+__device__ __forceinline__ float unif(uint32_t x) { return (float)(x >> 8) * 0x1.0p-24f; }
+__device__ __forceinline__ float unif16(uint32_t x16) { return (float)x16 * 0x1.0p-16f; }
+__device__ __forceinline__ void angle_sincos(float u, float* s, float* c) { __sincosf(fmaf(u, 6.28318531f, -3.14159265f), s, c); }
+
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+__device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    e = __fsub_rn(b, __fsub_rn(s, a));
+}
+
+// ---------------------------------------------------------------- constants
+struct CubeF {   // cube geometry in mm, growth 0 (geometry.rs:136-205)
+    float size, c0, pitch, half_d, t_pcb, gap, ptd, stem_r, clear_r, rod_hole, l_ext, cap_reach, cap_r, ap_r;
+    int32_t n, array, ent_axis, ent_side, ent_cell0, ent_cell1, ext_axis, ext_side, ext_cell0, ext_cell1;
+};
+
+struct PortM {
+    const float4* rec;       // 48 B records: {RF.xyz, 0} {DC.xyz (+ gate bias), cell conductor bits} {AC.xyz, 0}
+    int32_t nx, ny, nz, idle;
+    float u2v, inv_h;        // h / dt [m/s per cell/step], 1 / h [1/m]
+    float zret, zexit;       // Z_RETURN / h, Z_EXIT / h
+    double h;                // [m]
+};
+
+struct TMConst {
+    CubeF G;
+    const float4* crec[2];   // cube 32 B records {RF.xyz, 0} {DC.xyz, 0}: [0] splitter, [1] combiner
+    int32_t cn[3], pad0;
+    float clo[3], ch;        // grid origin and spacing [mm]
+    float cu2v, cinv_h;      // cube h / dt, 1 / h [1/m]
+    float seam_mm, lext_mm, ent_b, ent_c;   // entrance axis centre: along z, along x [mm]
+    float mouth_mm[9][2];
+    double clo_d[3], ch_d, seam_m, axis_m, mouth_m[9][2];
+    PortM port[9];
+    float qmdt2[8], nsd[8], mr[8];   // per species: q/m dt^2 [m per V/m], n sigma dt, M/(m+M)
+    float s_gas, pad1;
+    double dt;
+};
+
+struct MTracks {   // mixed-precision track state (structure of arrays)
+    float *xh, *xl, *uh, *ul;   // [3][n] each
+    int32_t *region, *last, *sp;
+    uint64_t* key;
+};
+
+// ---------------------------------------------------------------- cube geometry in FP32
+__device__ __forceinline__ float latf(const CubeF& G, int i) { return G.c0 + G.pitch * (float)i; }
+__device__ __forceinline__ int round_idxf(float v, int hi) {   // v.round() as usize, clamped (NaN -> 0)
+    const float r = roundf(v);
+    if (!(r > 0.0f)) return 0;
+    return r < (float)hi ? (int)r : hi;
+}
+__device__ __forceinline__ int nearest_portf(const CubeF& G, float x, float y) {   // geometry.rs:118-125
+    if (!G.array) return 0;
+    const float first = 0.5f * (latf(G, 2) + latf(G, 3));
+    return round_idxf((x - first) / (2.0f * G.pitch), 2) + 3 * round_idxf((y - first) / (2.0f * G.pitch), 2);
+}
+__device__ __forceinline__ float hypf2(float u, float v) { return sqrtf(fmaf(u, u, v * v)); }
+
+// any electrode at p (mm)?  (classify(p, 0) != FREE, geometry.rs:136-205)
+__device__ bool solid(const CubeF& G, const float p[3]) {
+    const float l = G.size;
+    const bool inside = p[0] >= -1e-12f && p[0] <= l + 1e-12f && p[1] >= -1e-12f && p[1] <= l + 1e-12f &&
+                        p[2] >= -1e-12f && p[2] <= l + 1e-12f;
+    for (int a = 0; a < 3; ++a) {
+        const int b = (a + 1) % 3, c = (a + 2) % 3;
+        for (int side = 0; side < 2; ++side) {
+            const float u = side == 0 ? p[a] : l - p[a];
+            int pid = 0, pc0 = 0, pc1 = 0;
+            if (G.ent_axis == a && G.ent_side == side) { pid = 3; pc0 = G.ent_cell0; pc1 = G.ent_cell1; }
+            else if (G.ext_axis == a && G.ext_side == side) {
+                pid = 4;
+                if (G.array) { const int i = nearest_portf(G, p[b], p[c]); pc0 = 2 + 2 * (i % 3); pc1 = 2 + 2 * (i / 3); }
+                else { pc0 = G.ext_cell0; pc1 = G.ext_cell1; }
+            }
+            const float cb = 0.5f * (latf(G, pc0) + latf(G, pc0 + 1)), cc = 0.5f * (latf(G, pc1) + latf(G, pc1 + 1));
+            if (u < 0.0f || (pid != 0 && u < 1e-12f)) {   // outside the wall: port rods and end cap
+                if (pid != 0) {
+                    if (u <= -G.cap_reach && hypf2(p[b] - cb, p[c] - cc) < G.cap_r) return true;
+                    if (u >= -G.l_ext)
+                        for (int m = 0; m < 4; ++m)
+                            if (hypf2(p[b] - latf(G, pc0 + (m >> 1)), p[c] - latf(G, pc1 + (m & 1))) < G.half_d) return true;
+                }
+                continue;
+            }
+            if (!inside || u > G.ptd) continue;
+            const int ib = round_idxf((p[b] - G.c0) / G.pitch, G.n - 1), ic = round_idxf((p[c] - G.c0) / G.pitch, G.n - 1);
+            int idx[3];
+            idx[a] = side == 0 ? 0 : G.n - 1;
+            idx[b] = ib;
+            idx[c] = ic;
+            bool valid = true;   // post_valid (geometry.rs:81-86): idx[a] is on this face already
+            for (int a2 = a + 1; a2 < 3; ++a2)
+                if (idx[a2] == 0 || idx[a2] == G.n - 1) valid = false;
+            const float dd = hypf2(p[b] - latf(G, ib), p[c] - latf(G, ic));
+            const bool rod = pid != 0 && valid && (unsigned)(ib - pc0) <= 1u && (unsigned)(ic - pc1) <= 1u;
+            const bool aperture = pid != 0 && hypf2(p[b] - cb, p[c] - cc) < G.ap_r;
+            if (rod && dd < G.half_d) return true;
+            if (u <= G.t_pcb && !(aperture || (valid && dd < (rod ? G.rod_hole : G.clear_r)))) return true;
+            if (valid && !rod) {
+                if (u <= G.t_pcb + G.gap && dd < G.stem_r) return true;
+                if (u >= G.t_pcb + G.gap && dd < G.half_d) return true;
+            }
+        }
+    }
+    return false;
+}
+
+// ---------------------------------------------------------------- fields
+__device__ __forceinline__ float lerp3(const float F[8], float tx, float ty, float tz) {
+    const float c00 = fmaf(tx, F[1] - F[0], F[0]), c10 = fmaf(tx, F[3] - F[2], F[2]);
+    const float c01 = fmaf(tx, F[5] - F[4], F[4]), c11 = fmaf(tx, F[7] - F[6], F[6]);
+    const float c0 = fmaf(ty, c10 - c00, c00), c1 = fmaf(ty, c11 - c01, c01);
+    return fmaf(tz, c1 - c0, c0);
+}
+
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+// cube: E = rf * RF + DC at the cell (ci, cj, ck), weights (tx, ty, tz)
+__device__ __forceinline__ void cube_e(const float4* __restrict__ rec, const int32_t cn[3], int ci, int cj, int ck, float tx,
+                                       float ty, float tz, float rf, float E[3]) {
+    const size_t sy = (size_t)cn[0], sz = (size_t)cn[0] * (size_t)cn[1];
+    const size_t base = (size_t)ci + sy * (size_t)cj + sz * (size_t)ck;
+    float F[3][8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const size_t o = 2 * (base + (size_t)(q & 1) + ((q & 2) ? sy : 0) + ((q & 4) ? sz : 0));
+        const float4 r = __ldg(rec + o), d = __ldg(rec + o + 1);
+        F[0][q] = fmaf(rf, r.x, d.x);
+        F[1][q] = fmaf(rf, r.y, d.y);
+        F[2][q] = fmaf(rf, r.z, d.z);
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) E[k] = lerp3(F[k], tx, ty, tz);
+}
+
+// port: E = rf * RF + ac * AC + DC at the cell
+__device__ __forceinline__ void port_e(const PortM& P, int ci, int cj, int ck, float tx, float ty, float tz, float rf, float ac,
+                                       float E[3]) {
+    const size_t sy = (size_t)P.nx, sz = (size_t)P.nx * (size_t)P.ny;
+    const size_t base = (size_t)ci + sy * (size_t)cj + sz * (size_t)ck;
+    float F[3][8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const size_t o = 3 * (base + (size_t)(q & 1) + ((q & 2) ? sy : 0) + ((q & 4) ? sz : 0));
+        const float4 r = __ldg(P.rec + o), d = __ldg(P.rec + o + 1), a = __ldg(P.rec + o + 2);
+        F[0][q] = fmaf(rf, r.x, fmaf(ac, a.x, d.x));
+        F[1][q] = fmaf(rf, r.y, fmaf(ac, a.y, d.y));
+        F[2][q] = fmaf(rf, r.z, fmaf(ac, a.z, d.z));
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) E[k] = lerp3(F[k], tx, ty, tz);
+}
+
+// double-float <-> FP64
+__device__ __forceinline__ double ddv(float h, float l) { return (double)h + (double)l; }
+__device__ __forceinline__ void splitd(double v, float& h, float& l) {
+    h = (float)v;
+    l = (float)(v - (double)h);
+}
+
+// FP64 physical state -> mixed state in the region's grid units
+__global__ void k_tm_load(TMConst C, Tracks64 T, MTracks M, uint32_t n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int r = T.region[i];
+    M.region[i] = r;
+    M.last[i] = T.last[i];
+    M.sp[i] = T.sp[i];
+    M.key[i] = T.rng[i];
+    if (r > R_COMBINE) return;
+    const double x[3] = {T.x[i], T.y[i], T.z[i]}, v[3] = {T.vx[i], T.vy[i], T.vz[i]};
+    for (int d = 0; d < 3; ++d) {
+        double g, u;
+        if (r == R_SPLIT || r == R_COMBINE) {
+            g = (x[d] * 1000.0 - C.clo_d[d]) / C.ch_d;
+            u = v[d] * C.dt * 1000.0 / C.ch_d;
+        } else {
+            g = x[d] / C.port[r - 1].h;
+            u = v[d] * C.dt / C.port[r - 1].h;
+        }
+        splitd(g, M.xh[(size_t)d * n + i], M.xl[(size_t)d * n + i]);
+        splitd(u, M.uh[(size_t)d * n + i], M.ul[(size_t)d * n + i]);
+    }
+}
+
+// mixed state -> FP64 physical state
+__global__ void k_tm_store(TMConst C, Tracks64 T, MTracks M, uint32_t n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int r = M.region[i];
+    T.region[i] = r;
+    T.last[i] = M.last[i];
+    if (r > R_COMBINE) return;   // finished tracks keep the state they left with
+    double x[3], v[3];
+    for (int d = 0; d < 3; ++d) {
+        const double g = ddv(M.xh[(size_t)d * n + i], M.xl[(size_t)d * n + i]);
+        const double u = ddv(M.uh[(size_t)d * n + i], M.ul[(size_t)d * n + i]);
+        if (r == R_SPLIT || r == R_COMBINE) {
+            x[d] = (C.clo_d[d] + g * C.ch_d) * 1e-3;
+            v[d] = u * C.ch_d * 1e-3 / C.dt;
+        } else {
+            x[d] = g * C.port[r - 1].h;
+            v[d] = u * C.port[r - 1].h / C.dt;
+        }
+    }
+    T.x[i] = x[0]; T.y[i] = x[1]; T.z[i] = x[2];
+    T.vx[i] = v[0]; T.vy[i] = v[1]; T.vz[i] = v[2];
+}
+
+// group the live tracks by region: list[r * n + k], one warp-aggregated atomic per region group
+__global__ void k_tm_bucket(const int32_t* __restrict__ region, uint32_t n, uint32_t* __restrict__ list,
+                            uint32_t* __restrict__ bcount) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int r = i < n ? region[i] : R_LOST;
+    const bool live = r <= R_COMBINE;
+    const unsigned lm = __ballot_sync(FULL, live);
+    if (!live) return;
+    const unsigned peers = __match_any_sync(lm, r);
+    const int leader = __ffs(peers) - 1;
+    const uint32_t lane = threadIdx.x & 31;
+    uint32_t base = 0;
+    if ((int)lane == leader) base = atomicAdd(&bcount[r], (uint32_t)__popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    list[(size_t)r * n + base + __popc(peers & ((1u << lane) - 1u))] = i;
+}
+
+// one chunk of global steps for every live track (one thread per track, grouped by region)
+__global__ void __launch_bounds__(128) k_tm_step(TMConst C, MTracks M, uint32_t n, const uint32_t* __restrict__ list,
+                                                 const uint32_t* __restrict__ bcount, const double* __restrict__ drive,
+                                                 uint64_t g0, uint32_t S, uint32_t* __restrict__ counts,
+                                                 unsigned long long* __restrict__ stepc) {
+    __shared__ uint32_t off[kBuckets + 1];
+    if (threadIdx.x == 0) {
+        uint32_t a = 0;
+        for (int r = 0; r < kBuckets; ++r) { off[r] = a; a += bcount[r]; }
+        off[kBuckets] = a;
+    }
+    __syncthreads();
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t n_cube = 0, n_port = 0, n_idle = 0;
+    if (t < off[kBuckets]) {
+        int r0 = 0;
+        while (r0 < kBuckets - 1 && t >= off[r0 + 1]) ++r0;
+        const uint32_t id = list[(size_t)r0 * n + (t - off[r0])];
+        int reg = r0, last = M.last[id];
+        const int sp = M.sp[id];
+        const uint64_t key = M.key[id];
+        const uint32_t k0 = (uint32_t)key, k1 = (uint32_t)(key >> 32);
+        float xh[3], xl[3], uh[3], ul[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            xh[d] = M.xh[(size_t)d * n + id]; xl[d] = M.xl[(size_t)d * n + id];
+            uh[d] = M.uh[(size_t)d * n + id]; ul[d] = M.ul[(size_t)d * n + id];
+        }
+        const float qmdt2 = C.qmdt2[sp], nsd = C.nsd[sp], mr = C.mr[sp];
+        uint4 rc = make_uint4(0, 0, 0, 0);
+        for (uint32_t k = 0; k < S && reg <= R_COMBINE; ++k) {
+            const uint64_t g = g0 + k;
+            if (k == 0 || (g & 3) == 0) rc = philox(k0, k1, (uint32_t)(g >> 2), (uint32_t)(g >> 34), 0u, 0u);
+            const double* dr = drive + (size_t)k * 10;
+            const float rf = (float)dr[0];
+            const bool cube = reg == R_SPLIT || reg == R_COMBINE;
+            float E[3], kick, u2v;
+            if (cube) {
+                const int ci = clampi(__float2int_rd(xh[0]), 0, C.cn[0] - 2), cj = clampi(__float2int_rd(xh[1]), 0, C.cn[1] - 2),
+                          ck = clampi(__float2int_rd(xh[2]), 0, C.cn[2] - 2);
+                // fields.rs:89-96 clamps the grid coordinate to the grid: weights clamped to [0, 1]
+                const float tx = __saturatef(__fadd_rn(__fsub_rn(xh[0], (float)ci), xl[0]));
+                const float ty = __saturatef(__fadd_rn(__fsub_rn(xh[1], (float)cj), xl[1]));
+                const float tz = __saturatef(__fadd_rn(__fsub_rn(xh[2], (float)ck), xl[2]));
+                cube_e(C.crec[reg == R_COMBINE ? 1 : 0], C.cn, ci, cj, ck, tx, ty, tz, rf, E);
+                kick = qmdt2 * C.cinv_h;
+                u2v = C.cu2v;
+                ++n_cube;
+            } else {
+                const PortM& P = C.port[reg - 1];
+                const int ci = clampi(__float2int_rd(xh[0]), 0, P.nx - 2), cj = clampi(__float2int_rd(xh[1]), 0, P.ny - 2),
+                          ck = clampi(__float2int_rd(xh[2]), 0, P.nz - 2);
+                const float tx = __fadd_rn(__fsub_rn(xh[0], (float)ci), xl[0]);
+                const float ty = __fadd_rn(__fsub_rn(xh[1], (float)cj), xl[1]);
+                const float tz = __fadd_rn(__fsub_rn(xh[2], (float)ck), xl[2]);
+                port_e(P, ci, cj, ck, tx, ty, tz, rf, (float)dr[reg], E);
+                kick = qmdt2 * P.inv_h;
+                u2v = P.u2v;
+                if (P.idle) ++n_idle;
+                else ++n_port;
+            }
+            // kick and drift, compensated (transport_step, lib.rs:90-103)
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                const float inc = __fadd_rn(__fmul_rn(kick, E[d]), ul[d]);
+                two_sum(uh[d], inc, uh[d], ul[d]);
+                float s, e;
+                fast_two_sum(xh[d], uh[d], s, e);
+                e = __fadd_rn(e, __fadd_rn(xl[d], ul[d]));
+                fast_two_sum(s, e, xh[d], xl[d]);
+            }
+            // null-collision thermal bath (world.rs:473-488): candidate if u0 < nsd (|v| + 6 s_gas)
+            {
+                const uint32_t q = (uint32_t)(g & 3);
+                const float u0 = unif(q == 0 ? rc.x : q == 1 ? rc.y : q == 2 ? rc.z : rc.w);
+                const float um2 = fmaf(uh[0], uh[0], fmaf(uh[1], uh[1], uh[2] * uh[2]));
+                const float ca = nsd * u2v, du = u0 - nsd * 6.0f * C.s_gas;
+                if (du < 0.0f || du * du < ca * ca * um2) {
+                    const uint4 r0 = philox(k0, k1, (uint32_t)g, (uint32_t)(g >> 32), 1u, 0u);
+                    const float v[3] = {uh[0] * u2v, uh[1] * u2v, uh[2] * u2v};
+                    const float bound = fmaf(sqrtf(um2), u2v, 6.0f * C.s_gas);
+                    const float g1 = sqrtf(-2.0f * __logf(fmaxf(unif(r0.x), 0x1.0p-25f)));
+                    const float g2 = sqrtf(-2.0f * __logf(fmaxf(unif(r0.y), 0x1.0p-25f)));
+                    float s1, c1, s2, c2;
+                    angle_sincos(unif16(r0.z >> 16), &s1, &c1);
+                    angle_sincos(unif16(r0.z & 0xffffu), &s2, &c2);
+                    const float gv[3] = {fmaf(-C.s_gas, g1 * c1, v[0]), fmaf(-C.s_gas, g1 * s1, v[1]),
+                                         fmaf(-C.s_gas, g2 * c2, v[2])};
+                    const float gl = sqrtf(fmaf(gv[0], gv[0], fmaf(gv[1], gv[1], gv[2] * gv[2])));
+                    if (unif16(r0.w >> 16) * bound < gl) {
+                        const float cth = 2.0f * unif16(r0.w & 0xffffu) - 1.0f;
+                        float sp_, cp_;
+                        angle_sincos(unif16(((r0.x & 0xffu) << 8) | (r0.y & 0xffu)), &sp_, &cp_);
+                        const float sn = sqrtf(fmaxf(0.0f, 1.0f - cth * cth));
+                        const float nn[3] = {sn * cp_, sn * sp_, cth};
+                        const float v2u = 1.0f / u2v;
+#pragma unroll
+                        for (int d = 0; d < 3; ++d) {
+                            uh[d] = fmaf(mr * gl, nn[d], fmaf(-mr, gv[d], v[d])) * v2u;
+                            ul[d] = 0.0f;
+                        }
+                    }
+                }
+            }
+            // routing (lib.rs:212-272)
+            if (cube) {
+                float p[3];
+#pragma unroll
+                for (int d = 0; d < 3; ++d) p[d] = fmaf(xh[d], C.ch, fmaf(xl[d], C.ch, C.clo[d]));
+                const float lo_in = C.G.ptd, hi_in = C.G.size - C.G.ptd;
+                const bool interior = p[0] > lo_in && p[0] < hi_in && p[1] > lo_in && p[1] < hi_in && p[2] > lo_in &&
+                                      p[2] < hi_in;
+                if (!interior && solid(C.G, p)) { reg = R_LOST; continue; }
+                if (p[2] > C.seam_mm) {
+                    const int i = nearest_portf(C.G, p[0], p[1]);
+                    if (hypf2(p[0] - C.mouth_mm[i][0], p[1] - C.mouth_mm[i][1]) < C.G.ap_r) {
+                        // enter (lib.rs:338-367) in FP64, then the port's grid units
+                        uint32_t* cnt = counts + (size_t)i * kNC;
+                        double x[3], v[3];
+                        for (int d = 0; d < 3; ++d) {
+                            x[d] = (C.clo_d[d] + ddv(xh[d], xl[d]) * C.ch_d) * 1e-3;
+                            v[d] = ddv(uh[d], ul[d]) * C.ch_d * 1e-3 / C.dt;
+                        }
+                        x[0] += C.axis_m - C.mouth_m[i][0];
+                        x[1] += C.axis_m - C.mouth_m[i][1];
+                        const double depth = x[2] - C.seam_m;
+                        if (reg == R_SPLIT) {
+                            x[2] = Z_RETURN + depth;
+                            atomicAdd(cnt + 0, 1u);
+                            if (last >= 0) {
+                                atomicAdd(cnt + 3, 1u);
+                                atomicAdd(cnt + 5 + last, 1u);
+                                if (last != i) atomicAdd(cnt + 4, 1u);
+                            }
+                        } else {
+                            x[2] = Z_EXIT - depth;
+                            v[2] = -v[2];
+                            atomicAdd(cnt + 14, 1u);
+                        }
+                        reg = 1 + i;
+                        const double h = C.port[i].h;
+                        for (int d = 0; d < 3; ++d) {
+                            splitd(x[d] / h, xh[d], xl[d]);
+                            splitd(v[d] * C.dt / h, uh[d], ul[d]);
+                        }
+                        continue;
+                    }
+                    if (p[2] > C.G.size) { reg = R_LOST; continue; }
+                }
+                if (p[1] > C.G.size && hypf2(p[0] - C.ent_c, p[2] - C.ent_b) >= C.G.ap_r) { reg = R_LOST; continue; }
+                if (p[1] > C.G.size + C.lext_mm) reg = reg == R_SPLIT ? 12 : 13;
+                else if (p[0] < 0.0f || p[1] < 0.0f || p[2] < 0.0f || p[0] > C.G.size) reg = R_LOST;
+            } else {
+                const int i = reg - 1;
+                const PortM& P = C.port[i];
+                uint32_t* cnt = counts + (size_t)i * kNC;
+                // is_crash (world.rs:309-314): outside the box, or the nearest node is a conductor
+                const int fi = __float2int_rd(xh[0]), fj = __float2int_rd(xh[1]), fk = __float2int_rd(xh[2]);
+                bool crash = xh[0] < 0.0f || xh[1] < 0.0f || xh[2] < 0.0f || xh[0] > (float)(P.nx - 1) ||
+                             xh[1] > (float)(P.ny - 1) || xh[2] > (float)(P.nz - 1);
+                if (!crash) {
+                    const int ci = clampi(fi, 0, P.nx - 2), cj = clampi(fj, 0, P.ny - 2), ck = clampi(fk, 0, P.nz - 2);
+                    const size_t base = (size_t)ci + (size_t)P.nx * ((size_t)cj + (size_t)P.ny * (size_t)ck);
+                    const uint32_t mask = __float_as_uint(__ldg(&P.rec[3 * base + 1].w));
+                    const uint32_t qn = (__fadd_rn(__fsub_rn(xh[0], (float)ci), xl[0]) >= 0.5f ? 1u : 0u) |
+                                        (__fadd_rn(__fsub_rn(xh[1], (float)cj), xl[1]) >= 0.5f ? 2u : 0u) |
+                                        (__fadd_rn(__fsub_rn(xh[2], (float)ck), xl[2]) >= 0.5f ? 4u : 0u);
+                    crash = (mask >> qn) & 1u;
+                }
+                if (crash) {
+                    reg = R_LOST;
+                    atomicAdd(cnt + 15, 1u);
+                } else if (xh[2] < P.zret || xh[2] > P.zexit) {
+                    // leave (lib.rs:368-385) in FP64, then the cube's grid units
+                    double x[3], v[3];
+                    for (int d = 0; d < 3; ++d) {
+                        x[d] = ddv(xh[d], xl[d]) * P.h;
+                        v[d] = ddv(uh[d], ul[d]) * P.h / C.dt;
+                    }
+                    x[0] += C.mouth_m[i][0] - C.axis_m;
+                    x[1] += C.mouth_m[i][1] - C.axis_m;
+                    if (x[2] < Z_RETURN) {
+                        x[2] = C.seam_m + x[2] - Z_RETURN;
+                        reg = R_SPLIT;
+                        last = i;
+                        atomicAdd(cnt + 1, 1u);
+                    } else {
+                        x[2] = C.seam_m - (x[2] - Z_EXIT);
+                        v[2] = -v[2];
+                        reg = R_COMBINE;
+                        last = -1;
+                        atomicAdd(cnt + 2, 1u);
+                        atomicAdd(cnt + 16 + sp, 1u);
+                    }
+                    for (int d = 0; d < 3; ++d) {
+                        splitd((x[d] * 1000.0 - C.clo_d[d]) / C.ch_d, xh[d], xl[d]);
+                        splitd(v[d] * C.dt * 1000.0 / C.ch_d, uh[d], ul[d]);
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            M.xh[(size_t)d * n + id] = xh[d]; M.xl[(size_t)d * n + id] = xl[d];
+            M.uh[(size_t)d * n + id] = uh[d]; M.ul[(size_t)d * n + id] = ul[d];
+        }
+        M.region[id] = reg;
+        M.last[id] = last;
+    }
+    // executed track-steps by region kind: one atomic per warp (every lane reaches this point)
+    n_cube = __reduce_add_sync(FULL, n_cube);
+    n_port = __reduce_add_sync(FULL, n_port);
+    n_idle = __reduce_add_sync(FULL, n_idle);
+    if ((threadIdx.x & 31) == 0) {
+        if (n_cube) atomicAdd(stepc + 0, (unsigned long long)n_cube);
+        if (n_port) atomicAdd(stepc + 1, (unsigned long long)n_port);
+        if (n_idle) atomicAdd(stepc + 2, (unsigned long long)n_idle);
+    }
+}
+
+// cube records: {RF.xyz, 0} {DC_region.xyz, 0}
+__global__ void k_tm_pack_cube(const float4* __restrict__ rf, const float4* __restrict__ dc, float4* __restrict__ rec,
+                               size_t nodes) {
+    const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nodes) return;
+    const float4 r = rf[q], d = dc[q];
+    rec[2 * q] = make_float4(r.x, r.y, r.z, 0.0f);
+    rec[2 * q + 1] = make_float4(d.x, d.y, d.z, 0.0f);
+}
+
+// port records: {RF.xyz, 0} {DC.xyz + bias * gate.xyz, conductor bits of the cell} {AC.xyz, 0}
+__global__ void k_tm_pack_port(const float4* __restrict__ rf, const float4* __restrict__ ac, const float4* __restrict__ dc,
+                               const float4* __restrict__ gate, float bias, int32_t nx, int32_t ny, int32_t nz,
+                               float4* __restrict__ rec) {
+    const size_t nodes = (size_t)nx * ny * nz;
+    const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nodes) return;
+    const float4 r = rf[q], d = dc[q], a = ac[q];
+    const float4 gt = bias != 0.0f ? gate[q] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const size_t sy = (size_t)nx, sz = (size_t)nx * (size_t)ny;
+    const int32_t i = (int32_t)(q % sy), j = (int32_t)((q / sy) % (size_t)ny), k = (int32_t)(q / sz);
+    uint32_t m = 0;
+    if (i < nx - 1 && j < ny - 1 && k < nz - 1)
+        for (int c = 0; c < 8; ++c)
+            m |= (rf[q + (size_t)(c & 1) + ((c & 2) ? sy : 0) + ((c & 4) ? sz : 0)].w > 0.5f ? 1u : 0u) << c;
+    rec[3 * q] = make_float4(r.x, r.y, r.z, 0.0f);
+    rec[3 * q + 1] = make_float4(fmaf(bias, gt.x, d.x), fmaf(bias, gt.y, d.y), fmaf(bias, gt.z, d.z), __uint_as_float(m));
+    rec[3 * q + 2] = make_float4(a.x, a.y, a.z, 0.0f);
+}
+
+}  // namespace
+
+struct State {
+    TMConst C;
+    std::vector<void*> allocs;
+    MTracks M{};
+    uint32_t cap = 0;
+    uint32_t* list = nullptr;
+    uint32_t* bcount = nullptr;
+};
+
+static void free_tracks(State* s) {
+    for (void* p : {(void*)s->M.xh, (void*)s->M.xl, (void*)s->M.uh, (void*)s->M.ul, (void*)s->M.region, (void*)s->M.last,
+                    (void*)s->M.sp, (void*)s->M.key, (void*)s->list})
+        if (p) cudaFree(p);
+    s->M = MTracks{};
+    s->list = nullptr;
+    s->cap = 0;
+}
+
+State* create(const mq_tandem_desc& d, const DevFields& f, cudaStream_t st, std::string& err) {
+    State* s = new (std::nothrow) State();
+    if (!s) { err = "out of host memory"; return nullptr; }
+    std::memset(&s->C, 0, sizeof(s->C));
+    TMConst& C = s->C;
+    auto fail = [&](const char* what, cudaError_t e) -> State* {
+        err = std::string(what) + ": " + cudaGetErrorString(e);
+        destroy(s);
+        return nullptr;
+    };
+    cudaError_t e;
+    // cube geometry in FP32 (growth 0)
+    const mq_cube_geom& g = d.cube;
+    CubeF& G = C.G;
+    G.size = (float)mqc::size(g);
+    G.c0 = (float)mqc::c0(g);
+    G.pitch = (float)g.pitch;
+    G.half_d = (float)(g.d / 2.0);
+    G.t_pcb = (float)g.t_pcb;
+    G.gap = (float)g.gap;
+    G.ptd = (float)mqc::post_top_depth(g);
+    G.stem_r = (float)g.stem_r;
+    G.clear_r = (float)g.clear_r;
+    G.rod_hole = (float)(g.d / 2.0 + g.rod_clear_extra);
+    G.l_ext = (float)g.l_ext;
+    G.cap_reach = (float)(g.l_ext + g.cap_gap);
+    G.cap_r = (float)g.cap_r;
+    G.ap_r = (float)g.ap_r;
+    G.n = g.n; G.array = g.array;
+    G.ent_axis = g.ent_axis; G.ent_side = g.ent_side; G.ent_cell0 = g.ent_cell[0]; G.ent_cell1 = g.ent_cell[1];
+    G.ext_axis = g.ext_axis; G.ext_side = g.ext_side; G.ext_cell0 = g.ext_cell[0]; G.ext_cell1 = g.ext_cell[1];
+    // cube grid and the two region DC sets
+    const size_t cn = (size_t)d.cube_dims[0] * d.cube_dims[1] * d.cube_dims[2];
+    for (int a = 0; a < 3; ++a) {
+        C.cn[a] = d.cube_dims[a];
+        C.clo[a] = (float)d.cube_lo_mm[a];
+        C.clo_d[a] = d.cube_lo_mm[a];
+    }
+    C.ch = (float)d.cube_h_mm;
+    C.ch_d = d.cube_h_mm;
+    C.cu2v = (float)(d.cube_h_mm * 1e-3 / d.dt);
+    C.cinv_h = (float)(1.0 / (d.cube_h_mm * 1e-3));
+    for (int r = 0; r < 2; ++r) {
+        void* p = nullptr;
+        if ((e = cudaMalloc(&p, cn * 32)) != cudaSuccess) return fail("cube records", e);
+        s->allocs.push_back(p);
+        C.crec[r] = static_cast<const float4*>(p);
+        k_tm_pack_cube<<<(unsigned)((cn + 255) / 256), 256, 0, st>>>(f.crf, f.cdc[r], static_cast<float4*>(p), cn);
+        if ((e = cudaGetLastError()) != cudaSuccess) return fail("cube pack", e);
+    }
+    // layout: seam, mouths, entrance axis
+    double seam = 0, size = 0, mouths[18], ent[2];
+    mq_tandem_layout(&d, &seam, &size, mouths);
+    mq_cube_port_axis(&d.cube, -1, ent);
+    C.seam_m = seam;
+    C.seam_mm = (float)(seam * 1000.0);
+    C.lext_mm = (float)g.l_ext;
+    C.ent_b = (float)ent[0];
+    C.ent_c = (float)ent[1];
+    C.axis_m = d.ch_axis_mm * 1e-3;
+    for (int i = 0; i < 9; ++i)
+        for (int k = 0; k < 2; ++k) {
+            C.mouth_m[i][k] = mouths[2 * i + k];
+            C.mouth_mm[i][k] = (float)(mouths[2 * i + k] * 1000.0);
+        }
+    // ports: one packed record array per distinct (grid arrays, idle)
+    struct Key { const float4 *rf, *ac, *dc, *gate; int idle; const float4* rec; };
+    std::vector<Key> made;
+    for (int i = 0; i < 9; ++i) {
+        const mq_tandem_port& tp = d.port[i];
+        PortM& P = C.port[i];
+        P.nx = tp.dims[0]; P.ny = tp.dims[1]; P.nz = tp.dims[2];
+        P.idle = tp.tone_khz == 0.0;
+        P.h = tp.h;
+        P.u2v = (float)(tp.h / d.dt);
+        P.inv_h = (float)(1.0 / tp.h);
+        P.zret = (float)(Z_RETURN / tp.h);
+        P.zexit = (float)(Z_EXIT / tp.h);
+        const Key k{f.prf[i], f.pac[i], f.pdc[i], f.pgate[i], P.idle, nullptr};
+        for (const Key& m : made)
+            if (m.rf == k.rf && m.ac == k.ac && m.dc == k.dc && m.gate == k.gate && m.idle == k.idle) P.rec = m.rec;
+        if (!P.rec) {
+            const size_t nodes = (size_t)P.nx * P.ny * P.nz;
+            void* p = nullptr;
+            if ((e = cudaMalloc(&p, nodes * 48)) != cudaSuccess) return fail("port records", e);
+            s->allocs.push_back(p);
+            k_tm_pack_port<<<(unsigned)((nodes + 255) / 256), 256, 0, st>>>(f.prf[i], f.pac[i], f.pdc[i], f.pgate[i],
+                                                                            P.idle ? (float)d.gate_bias_v : 0.0f, P.nx,
+                                                                            P.ny, P.nz, static_cast<float4*>(p));
+            if ((e = cudaGetLastError()) != cudaSuccess) return fail("port pack", e);
+            P.rec = static_cast<const float4*>(p);
+            Key km = k;
+            km.rec = P.rec;
+            made.push_back(km);
+        }
+    }
+    // species (SpPhys::new, world.rs:342-347) and the gas
+    const double mg = 28.0 * mqp::AMU;
+    const double ngas = d.pressure_pa / (mqp::KB * d.temp_k);
+    C.s_gas = (float)std::sqrt(mqp::KB * d.temp_k / mg);
+    C.dt = d.dt;
+    for (int k = 0; k < d.nspecies && k < 8; ++k) {
+        const double m = d.species[k].mass * mqp::AMU;
+        C.qmdt2[k] = (float)(d.species[k].z * mqp::QE / m * d.dt * d.dt);
+        C.nsd[k] = (float)(ngas * d.species[k].ccs * 1e-20 * d.dt);
+        C.mr[k] = (float)(mg / (m + mg));
+    }
+    if ((e = cudaMalloc(&s->bcount, kBuckets * sizeof(uint32_t))) != cudaSuccess) return fail("bucket counters", e);
+    return s;
+}
+
+void destroy(State* s) {
+    if (!s) return;
+    free_tracks(s);
+    for (void* p : s->allocs) cudaFree(p);
+    if (s->bcount) cudaFree(s->bcount);
+    delete s;
+}
+
+static cudaError_t reserve(State* s, uint32_t n) {
+    if (s->cap >= n && s->M.xh) return cudaSuccess;
+    free_tracks(s);
+    cudaError_t e;
+    const size_t m = n ? n : 1;
+    if ((e = cudaMalloc(&s->M.xh, 3 * m * sizeof(float))) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&s->M.xl, 3 * m * sizeof(float))) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&s->M.uh, 3 * m * sizeof(float))) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&s->M.ul, 3 * m * sizeof(float))) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&s->M.region, m * sizeof(int32_t))) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&s->M.last, m * sizeof(int32_t))) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&s->M.sp, m * sizeof(int32_t))) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&s->M.key, m * sizeof(uint64_t))) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&s->list, (size_t)kBuckets * m * sizeof(uint32_t))) != cudaSuccess) return e;
+    s->cap = n;
+    return cudaSuccess;
+}
+
+cudaError_t load(State* s, const Tracks64& tr, uint32_t n, cudaStream_t st, uint32_t* launches) {
+    cudaError_t e = reserve(s, n);
+    if (e != cudaSuccess) return e;
+    if (!n) return cudaSuccess;
+    k_tm_load<<<(n + 127) / 128, 128, 0, st>>>(s->C, tr, s->M, n);
+    ++*launches;
+    return cudaGetLastError();
+}
+
+cudaError_t store(State* s, const Tracks64& tr, uint32_t n, cudaStream_t st, uint32_t* launches) {
+    if (!n) return cudaSuccess;
+    k_tm_store<<<(n + 127) / 128, 128, 0, st>>>(s->C, tr, s->M, n);
+    ++*launches;
+    return cudaGetLastError();
+}
+
+cudaError_t run(State* s, uint32_t n, const double* drive, uint64_t step0, uint64_t k, uint32_t* counts,
+                unsigned long long* stepc, cudaStream_t st, uint32_t* launches) {
+    cudaError_t e;
+    if (!n) return cudaSuccess;
+    const unsigned grid = (n + 127) / 128;
+    for (uint64_t q = 0; q < k; q += kChunk) {
+        const uint32_t S = (uint32_t)(k - q < kChunk ? k - q : kChunk);
+        if ((e = cudaMemsetAsync(s->bcount, 0, kBuckets * sizeof(uint32_t), st)) != cudaSuccess) return e;
+        k_tm_bucket<<<grid, 128, 0, st>>>(s->M.region, n, s->list, s->bcount);
+        k_tm_step<<<grid, 128, 0, st>>>(s->C, s->M, n, s->list, s->bcount, drive + q * 10, step0 + q, S, counts, stepc);
+        *launches += 2;
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+}  // namespace mqtm

@@ -349,12 +349,15 @@ class TandemModel:
     ``channel``: channel basis fields (default: the calibrated S14 world, ``Geom.s14()``) shared
     by the nine ports unless ``port_fields`` (nine ``Fields``) or ``port_grids`` (nine
     ``PortGrid``) give ports grids of their own; arrays shared between ports are uploaded once.
-    ``cube_h``: cube grid spacing target in mm (default 0.52 fine / 1.04 coarse)."""
+    ``cube_h``: cube grid spacing target in mm (default 0.52 fine / 1.04 coarse).
+    ``precision``: ``MQ_PREC_F64`` (the bit-exact FP64 twin) or ``MQ_PREC_MIXED`` (FP32 fields,
+    compensated FP32 state, counter-based collisions: statistically equivalent, much faster)."""
 
     def __init__(self, tones=DEFAULT_TONES, n: int = 180, seed: int = 486, fine: bool = False,
                  mouth_start: bool = True, *, channel: Fields | None = None, port_fields=None,
                  port_grids=None, cube_h: float | None = None, preset: TandemPreset | None = None,
-                 device: int = 0, dc_cal=DC_CAL, cube_tol: float = 1e-7):
+                 device: int = 0, dc_cal=DC_CAL, cube_tol: float = 1e-7, precision: int = N.MQ_PREC_F64):
+        self.precision = int(precision)
         self.tones = tuple(float(t) for t in tones)
         assert len(self.tones) == 9
         self.preset = preset or TandemPreset.fig5()
@@ -414,6 +417,7 @@ class TandemModel:
         d.v_rf, d.f_rf, d.pressure_pa, d.temp_k, d.dt = (self.preset.v_rf, F_RF, self.preset.pressure_pa,
                                                          self.preset.temp_k, DT)
         d.gate_bias_v = GATE_BIAS_V
+        d.precision = self.precision
         d.nspecies = len(self.preset.species)
         for k, s in enumerate(self.preset.species):
             d.species[k].mass, d.species[k].z, d.species[k].ccs, d.species[k].weight = s.mass, s.z, s.ccs, s.weight

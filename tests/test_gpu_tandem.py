@@ -135,3 +135,64 @@ def test_port_track_advances_like_the_fp64_channel_engine(tandem_small, s14_coar
         assert abs(getattr(ions, a)[0] - getattr(tr, a)[0]) < 1e-7
     assert int(ions.rng[0]) == int(tr.rng[0])
     m.close()
+
+
+# ------------------------------------------------------------------ the mixed-precision tandem engine
+
+
+def _region_counts(m):
+    return np.bincount(m.tracks.region, minlength=14)
+
+
+def test_tandem_mixed_deterministic(tandem_small):
+    a = tandem_small(n=3000, seed=21, precision=mq.PREC_MIXED)
+    b = tandem_small(n=3000, seed=21, precision=mq.PREC_MIXED)
+    for m in (a, b):
+        m.advance(7000)
+    _same_tracks(a.tracks, b.tracks)
+    assert np.array_equal(a.counts_array(), b.counts_array())
+    assert a.counts_array()[:, 0].sum() > 0
+    a.close()
+    b.close()
+
+
+def test_tandem_mixed_collision_free_tracks_fp64(tandem_small):
+    """Without gas the mixed engine follows the FP64 kernel: after 400 steps ≥ 99% of the tracks
+    are in the same region, at the same place to 1e-6 m and the same velocity to 1e-4 relative."""
+    fig5 = mq.TandemPreset.fig5()
+    vac = mq.TandemPreset(species=fig5.species, pressure_pa=0.0)
+    a = tandem_small(n=2000, seed=77, preset=vac)
+    b = tandem_small(n=2000, seed=77, preset=vac, precision=mq.PREC_MIXED)
+    for m in (a, b):
+        m.advance(400)
+    same = a.tracks.region == b.tracks.region
+    assert same.mean() >= 0.99
+    live = same & (a.tracks.region <= 10)
+    assert live.sum() > 1000
+    for k in ("x", "y", "z"):
+        assert np.max(np.abs(getattr(a.tracks, k)[live] - getattr(b.tracks, k)[live])) < 1e-6
+    va = np.stack([a.tracks.vx, a.tracks.vy, a.tracks.vz])[:, live]
+    vb = np.stack([b.tracks.vx, b.tracks.vy, b.tracks.vz])[:, live]
+    assert np.max(np.linalg.norm(va - vb, axis=0) / np.linalg.norm(va, axis=0)) < 1e-4
+    a.close()
+    b.close()
+
+
+def test_tandem_mixed_counts_match_fp64(tandem_small):
+    """With gas the two engines draw different random numbers; their census and per-port
+    counts agree within a few Poisson standard deviations."""
+    a = tandem_small(n=20000, seed=3)
+    b = tandem_small(n=20000, seed=3, precision=mq.PREC_MIXED)
+    for m in (a, b):
+        m.advance(20000)
+    ca, cb = a.counts_array().astype(float), b.counts_array().astype(float)
+    for col in (0, 1, 2, 15):   # entered, returned, forwarded, lost: summed over ports
+        x, y = ca[:, col].sum(), cb[:, col].sum()
+        assert abs(x - y) <= 4.0 * np.sqrt(x + y) + 10, (col, x, y)
+    ra, rb = _region_counts(a), _region_counts(b)
+    for x, y in ((ra[0], rb[0]), (ra[1:10].sum(), rb[1:10].sum()), (ra[10], rb[10]), (ra[11], rb[11])):
+        assert abs(x - y) <= 4.0 * np.sqrt(x + y) + 10, (x, y)
+    sa, sb = a.last_stats, b.last_stats
+    assert abs(sa.track_steps - sb.track_steps) <= 0.02 * sa.track_steps
+    a.close()
+    b.close()
