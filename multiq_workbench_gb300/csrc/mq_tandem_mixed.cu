@@ -9,7 +9,8 @@
 //     (cube grid in mm, or the port's grid); region changes convert through FP64 with
 //     trapsim's enter / leave arithmetic (lib.rs:338-385);
 //   * fields as interleaved node records: cube {RF, region DC} 32 B, port {RF, DC (+ gate
-//     bias on idle ports), AC} 48 B with the cell's conductor bits in a spare word;
+//     bias on idle ports), AC} 48 B with the cell's conductor bits in a spare word; the 8
+//     corners of the track's cell are held in registers and reloaded on a cell change;
 //   * drive values per global step read (as FP32) from the FP64 engine's drive table; thermal
 //     collisions with Philox-4x32-10 keyed by the track key and the global step (all lanes
 //     share the global step, so the generator runs warp-uniformly);
@@ -168,40 +169,56 @@ __device__ __forceinline__ float lerp3(const float F[8], float tx, float ty, flo
 
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
-// cube: E = rf * RF + DC at the cell (ci, cj, ck), weights (tx, ty, tz)
-__device__ __forceinline__ void cube_e(const float4* __restrict__ rec, const int32_t cn[3], int ci, int cj, int ck, float tx,
-                                       float ty, float tz, float rf, float E[3]) {
+// Register cache of the track's cell: the 8 corners x {RF, DC, AC} of its region's grid,
+// reloaded only when the track changes cell or region (cube cells leave A unused).
+struct TCell {
+    float R[3][8], D[3][8], A[3][8];   // corner q = a + 2b + 4c
+    int32_t ci, cj, ck, reg;
+    uint32_t mask;                      // port: conductor bit per corner
+};
+
+__device__ __forceinline__ void load_cube(const float4* __restrict__ rec, const int32_t cn[3], int ci, int cj, int ck,
+                                          TCell& c) {
     const size_t sy = (size_t)cn[0], sz = (size_t)cn[0] * (size_t)cn[1];
     const size_t base = (size_t)ci + sy * (size_t)cj + sz * (size_t)ck;
-    float F[3][8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
         const size_t o = 2 * (base + (size_t)(q & 1) + ((q & 2) ? sy : 0) + ((q & 4) ? sz : 0));
         const float4 r = __ldg(rec + o), d = __ldg(rec + o + 1);
-        F[0][q] = fmaf(rf, r.x, d.x);
-        F[1][q] = fmaf(rf, r.y, d.y);
-        F[2][q] = fmaf(rf, r.z, d.z);
+        c.R[0][q] = r.x; c.R[1][q] = r.y; c.R[2][q] = r.z;
+        c.D[0][q] = d.x; c.D[1][q] = d.y; c.D[2][q] = d.z;
     }
-#pragma unroll
-    for (int k = 0; k < 3; ++k) E[k] = lerp3(F[k], tx, ty, tz);
+    c.mask = 0;
 }
 
-// port: E = rf * RF + ac * AC + DC at the cell
-__device__ __forceinline__ void port_e(const PortM& P, int ci, int cj, int ck, float tx, float ty, float tz, float rf, float ac,
-                                       float E[3]) {
+__device__ __forceinline__ void load_port(const PortM& P, int ci, int cj, int ck, TCell& c) {
     const size_t sy = (size_t)P.nx, sz = (size_t)P.nx * (size_t)P.ny;
     const size_t base = (size_t)ci + sy * (size_t)cj + sz * (size_t)ck;
-    float F[3][8];
+    uint32_t m = 0;
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
         const size_t o = 3 * (base + (size_t)(q & 1) + ((q & 2) ? sy : 0) + ((q & 4) ? sz : 0));
         const float4 r = __ldg(P.rec + o), d = __ldg(P.rec + o + 1), a = __ldg(P.rec + o + 2);
-        F[0][q] = fmaf(rf, r.x, fmaf(ac, a.x, d.x));
-        F[1][q] = fmaf(rf, r.y, fmaf(ac, a.y, d.y));
-        F[2][q] = fmaf(rf, r.z, fmaf(ac, a.z, d.z));
+        c.R[0][q] = r.x; c.R[1][q] = r.y; c.R[2][q] = r.z;
+        c.D[0][q] = d.x; c.D[1][q] = d.y; c.D[2][q] = d.z;
+        c.A[0][q] = a.x; c.A[1][q] = a.y; c.A[2][q] = a.z;
+        if (q == 0) m = __float_as_uint(d.w);
     }
-#pragma unroll
-    for (int k = 0; k < 3; ++k) E[k] = lerp3(F[k], tx, ty, tz);
+    c.mask = m;
+}
+
+// the cell of grid position x (clamped to the grid), reloading the cache when it changes
+__device__ __forceinline__ void cell_for(const TMConst& C, int reg, const float xh[3], TCell& c) {
+    const bool cube = reg == R_SPLIT || reg == R_COMBINE;
+    const int nx = cube ? C.cn[0] : C.port[reg - 1].nx, ny = cube ? C.cn[1] : C.port[reg - 1].ny,
+              nz = cube ? C.cn[2] : C.port[reg - 1].nz;
+    const int ci = clampi(__float2int_rd(xh[0]), 0, nx - 2), cj = clampi(__float2int_rd(xh[1]), 0, ny - 2),
+              ck = clampi(__float2int_rd(xh[2]), 0, nz - 2);
+    if (ci != c.ci || cj != c.cj || ck != c.ck || reg != c.reg) {
+        if (cube) load_cube(C.crec[reg == R_COMBINE ? 1 : 0], C.cn, ci, cj, ck, c);
+        else load_port(C.port[reg - 1], ci, cj, ck, c);
+        c.ci = ci; c.cj = cj; c.ck = ck; c.reg = reg;
+    }
 }
 
 // double-float <-> FP64
@@ -278,10 +295,10 @@ __global__ void k_tm_bucket(const int32_t* __restrict__ region, uint32_t n, uint
 }
 
 // one chunk of global steps for every live track (one thread per track, grouped by region)
-__global__ void __launch_bounds__(128) k_tm_step(TMConst C, MTracks M, uint32_t n, const uint32_t* __restrict__ list,
-                                                 const uint32_t* __restrict__ bcount, const double* __restrict__ drive,
-                                                 uint64_t g0, uint32_t S, uint32_t* __restrict__ counts,
-                                                 unsigned long long* __restrict__ stepc) {
+__global__ void __launch_bounds__(128, 3) k_tm_step(TMConst C, MTracks M, uint32_t n, const uint32_t* __restrict__ list,
+                                                    const uint32_t* __restrict__ bcount, const double* __restrict__ drive,
+                                                    uint64_t g0, uint32_t S, uint32_t* __restrict__ counts,
+                                                    unsigned long long* __restrict__ stepc) {
     __shared__ uint32_t off[kBuckets + 1];
     if (threadIdx.x == 0) {
         uint32_t a = 0;
@@ -306,6 +323,10 @@ __global__ void __launch_bounds__(128) k_tm_step(TMConst C, MTracks M, uint32_t 
             uh[d] = M.uh[(size_t)d * n + id]; ul[d] = M.ul[(size_t)d * n + id];
         }
         const float qmdt2 = C.qmdt2[sp], nsd = C.nsd[sp], mr = C.mr[sp];
+        TCell c;
+        c.ci = c.cj = c.ck = -1;
+        c.reg = -1;
+        cell_for(C, reg, xh, c);
         uint4 rc = make_uint4(0, 0, 0, 0);
         for (uint32_t k = 0; k < S && reg <= R_COMBINE; ++k) {
             const uint64_t g = g0 + k;
@@ -314,25 +335,28 @@ __global__ void __launch_bounds__(128) k_tm_step(TMConst C, MTracks M, uint32_t 
             const float rf = (float)dr[0];
             const bool cube = reg == R_SPLIT || reg == R_COMBINE;
             float E[3], kick, u2v;
+            {
+                float tx = __fadd_rn(__fsub_rn(xh[0], (float)c.ci), xl[0]);
+                float ty = __fadd_rn(__fsub_rn(xh[1], (float)c.cj), xl[1]);
+                float tz = __fadd_rn(__fsub_rn(xh[2], (float)c.ck), xl[2]);
+                if (cube) {   // fields.rs:89-96 clamps the grid coordinate to the grid
+                    tx = __saturatef(tx); ty = __saturatef(ty); tz = __saturatef(tz);
+                }
+                const float ac = cube ? 0.0f : (float)dr[reg];
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    float F[8];
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) F[q] = cube ? fmaf(rf, c.R[d][q], c.D[d][q]) : fmaf(rf, c.R[d][q], fmaf(ac, c.A[d][q], c.D[d][q]));
+                    E[d] = lerp3(F, tx, ty, tz);
+                }
+            }
             if (cube) {
-                const int ci = clampi(__float2int_rd(xh[0]), 0, C.cn[0] - 2), cj = clampi(__float2int_rd(xh[1]), 0, C.cn[1] - 2),
-                          ck = clampi(__float2int_rd(xh[2]), 0, C.cn[2] - 2);
-                // fields.rs:89-96 clamps the grid coordinate to the grid: weights clamped to [0, 1]
-                const float tx = __saturatef(__fadd_rn(__fsub_rn(xh[0], (float)ci), xl[0]));
-                const float ty = __saturatef(__fadd_rn(__fsub_rn(xh[1], (float)cj), xl[1]));
-                const float tz = __saturatef(__fadd_rn(__fsub_rn(xh[2], (float)ck), xl[2]));
-                cube_e(C.crec[reg == R_COMBINE ? 1 : 0], C.cn, ci, cj, ck, tx, ty, tz, rf, E);
                 kick = qmdt2 * C.cinv_h;
                 u2v = C.cu2v;
                 ++n_cube;
             } else {
                 const PortM& P = C.port[reg - 1];
-                const int ci = clampi(__float2int_rd(xh[0]), 0, P.nx - 2), cj = clampi(__float2int_rd(xh[1]), 0, P.ny - 2),
-                          ck = clampi(__float2int_rd(xh[2]), 0, P.nz - 2);
-                const float tx = __fadd_rn(__fsub_rn(xh[0], (float)ci), xl[0]);
-                const float ty = __fadd_rn(__fsub_rn(xh[1], (float)cj), xl[1]);
-                const float tz = __fadd_rn(__fsub_rn(xh[2], (float)ck), xl[2]);
-                port_e(P, ci, cj, ck, tx, ty, tz, rf, (float)dr[reg], E);
                 kick = qmdt2 * P.inv_h;
                 u2v = P.u2v;
                 if (P.idle) ++n_idle;
@@ -422,6 +446,7 @@ __global__ void __launch_bounds__(128) k_tm_step(TMConst C, MTracks M, uint32_t 
                             splitd(x[d] / h, xh[d], xl[d]);
                             splitd(v[d] * C.dt / h, uh[d], ul[d]);
                         }
+                        cell_for(C, reg, xh, c);
                         continue;
                     }
                     if (p[2] > C.G.size) { reg = R_LOST; continue; }
@@ -429,22 +454,20 @@ __global__ void __launch_bounds__(128) k_tm_step(TMConst C, MTracks M, uint32_t 
                 if (p[1] > C.G.size && hypf2(p[0] - C.ent_c, p[2] - C.ent_b) >= C.G.ap_r) { reg = R_LOST; continue; }
                 if (p[1] > C.G.size + C.lext_mm) reg = reg == R_SPLIT ? 12 : 13;
                 else if (p[0] < 0.0f || p[1] < 0.0f || p[2] < 0.0f || p[0] > C.G.size) reg = R_LOST;
+                else cell_for(C, reg, xh, c);
             } else {
                 const int i = reg - 1;
                 const PortM& P = C.port[i];
                 uint32_t* cnt = counts + (size_t)i * kNC;
                 // is_crash (world.rs:309-314): outside the box, or the nearest node is a conductor
-                const int fi = __float2int_rd(xh[0]), fj = __float2int_rd(xh[1]), fk = __float2int_rd(xh[2]);
                 bool crash = xh[0] < 0.0f || xh[1] < 0.0f || xh[2] < 0.0f || xh[0] > (float)(P.nx - 1) ||
                              xh[1] > (float)(P.ny - 1) || xh[2] > (float)(P.nz - 1);
                 if (!crash) {
-                    const int ci = clampi(fi, 0, P.nx - 2), cj = clampi(fj, 0, P.ny - 2), ck = clampi(fk, 0, P.nz - 2);
-                    const size_t base = (size_t)ci + (size_t)P.nx * ((size_t)cj + (size_t)P.ny * (size_t)ck);
-                    const uint32_t mask = __float_as_uint(__ldg(&P.rec[3 * base + 1].w));
-                    const uint32_t qn = (__fadd_rn(__fsub_rn(xh[0], (float)ci), xl[0]) >= 0.5f ? 1u : 0u) |
-                                        (__fadd_rn(__fsub_rn(xh[1], (float)cj), xl[1]) >= 0.5f ? 2u : 0u) |
-                                        (__fadd_rn(__fsub_rn(xh[2], (float)ck), xl[2]) >= 0.5f ? 4u : 0u);
-                    crash = (mask >> qn) & 1u;
+                    cell_for(C, reg, xh, c);
+                    const uint32_t qn = (__fadd_rn(__fsub_rn(xh[0], (float)c.ci), xl[0]) >= 0.5f ? 1u : 0u) |
+                                        (__fadd_rn(__fsub_rn(xh[1], (float)c.cj), xl[1]) >= 0.5f ? 2u : 0u) |
+                                        (__fadd_rn(__fsub_rn(xh[2], (float)c.ck), xl[2]) >= 0.5f ? 4u : 0u);
+                    crash = (c.mask >> qn) & 1u;
                 }
                 if (crash) {
                     reg = R_LOST;
@@ -475,6 +498,7 @@ __global__ void __launch_bounds__(128) k_tm_step(TMConst C, MTracks M, uint32_t 
                         splitd((x[d] * 1000.0 - C.clo_d[d]) / C.ch_d, xh[d], xl[d]);
                         splitd(v[d] * C.dt * 1000.0 / C.ch_d, uh[d], ul[d]);
                     }
+                    cell_for(C, reg, xh, c);
                 }
             }
         }
