@@ -465,21 +465,28 @@ mq_status mq_tandem_advance(mq_tandem* t, mq_tracks* tr, size_t n, uint64_t step
     uint64_t per = n ? ((uint64_t)1 << 27) / n : tab;
     per = per < 32 ? 32 : (per > 4096 ? 4096 : per);
     std::vector<double> dtab(tab * 10);
+    std::vector<float> ftab(t->mix ? tab * 10 : 0);
     uint32_t launches = 0;
     uint64_t h2d = tb + cnt.size() * 4;
     for (uint64_t s = 0; s < steps || s == 0; s += tab) {
         const uint64_t k = steps - s < tab ? steps - s : tab;
         drive_table(t->desc, step0 + s, k, dtab.data());
         // pageable source: the call returns once the host buffer has been staged, so it may be refilled next
-        if (k) TCK(cudaMemcpyAsync(t->drive, dtab.data(), k * 10 * 8, cudaMemcpyHostToDevice, t->st), "drive upload");
-        h2d += k * 10 * 8;
+        if (t->mix) {   // the mixed engine reads the drive as FP32 (no FP64 conversions in its step loop)
+            for (uint64_t q = 0; q < k * 10; ++q) ftab[q] = (float)dtab[q];
+            if (k) TCK(cudaMemcpyAsync(t->drive, ftab.data(), k * 10 * 4, cudaMemcpyHostToDevice, t->st), "drive upload");
+            h2d += k * 10 * 4;
+        } else {
+            if (k) TCK(cudaMemcpyAsync(t->drive, dtab.data(), k * 10 * 8, cudaMemcpyHostToDevice, t->st), "drive upload");
+            h2d += k * 10 * 8;
+        }
         if (s == 0) {
             TCK(cudaEventRecord(t->ev[0], t->st), "event");   // times the kernels (and later table blocks)
             if (t->mix) TCK(mqtm::load(t->mix, T64, (uint32_t)n, t->st, &launches), "mixed tandem load");
         }
         if (!steps) break;
         if (t->mix) {
-            TCK(mqtm::run(t->mix, (uint32_t)n, (const double*)t->drive, step0 + s, k, t->counts, t->stepc, t->st, &launches),
+            TCK(mqtm::run(t->mix, (uint32_t)n, (const float*)t->drive, step0 + s, k, t->counts, t->stepc, t->st, &launches),
                 "mixed tandem kernel");
             continue;
         }

@@ -29,9 +29,9 @@ State* create(const mq_tandem_desc& d, const DevFields& f, cudaStream_t st, std:
 void destroy(State* s);
 // FP64 device tracks -> the engine's mixed state (n tracks)
 cudaError_t load(State* s, const Tracks64& tr, uint32_t n, cudaStream_t st, uint32_t* launches);
-// advance the mixed state by k global steps (drive: k x 10 doubles, RF + nine tones) starting at
+// advance the mixed state by k global steps (drive: k x 10 floats, RF + nine tones) starting at
 // global step step0; counts (9 x 21 u32) and stepc (3 u64) accumulate on the device
-cudaError_t run(State* s, uint32_t n, const double* drive, uint64_t step0, uint64_t k, uint32_t* counts,
+cudaError_t run(State* s, uint32_t n, const float* drive, uint64_t step0, uint64_t k, uint32_t* counts,
                 unsigned long long* stepc, cudaStream_t st, uint32_t* launches);
 // the engine's mixed state -> FP64 device tracks
 cudaError_t store(State* s, const Tracks64& tr, uint32_t n, cudaStream_t st, uint32_t* launches);

@@ -11,7 +11,7 @@
 //   * fields as interleaved node records: cube {RF, region DC} 32 B, port {RF, DC (+ gate
 //     bias on idle ports), AC} 48 B with the cell's conductor bits in a spare word; the 8
 //     corners of the track's cell are held in registers and reloaded on a cell change;
-//   * drive values per global step read (as FP32) from the FP64 engine's drive table; thermal
+//   * drive values per global step from the FP64 engine's drive table, rounded to FP32; thermal
 //     collisions with Philox-4x32-10 keyed by the track key and the global step (all lanes
 //     share the global step, so the generator runs warp-uniformly);
 //   * cube losses by the geometry test in FP32, skipped in the interior box where every
@@ -296,7 +296,7 @@ __global__ void k_tm_bucket(const int32_t* __restrict__ region, uint32_t n, uint
 
 // one chunk of global steps for every live track (one thread per track, grouped by region)
 __global__ void __launch_bounds__(128, 3) k_tm_step(TMConst C, MTracks M, uint32_t n, const uint32_t* __restrict__ list,
-                                                    const uint32_t* __restrict__ bcount, const double* __restrict__ drive,
+                                                    const uint32_t* __restrict__ bcount, const float* __restrict__ drive,
                                                     uint64_t g0, uint32_t S, uint32_t* __restrict__ counts,
                                                     unsigned long long* __restrict__ stepc) {
     __shared__ uint32_t off[kBuckets + 1];
@@ -331,8 +331,8 @@ __global__ void __launch_bounds__(128, 3) k_tm_step(TMConst C, MTracks M, uint32
         for (uint32_t k = 0; k < S && reg <= R_COMBINE; ++k) {
             const uint64_t g = g0 + k;
             if (k == 0 || (g & 3) == 0) rc = philox(k0, k1, (uint32_t)(g >> 2), (uint32_t)(g >> 34), 0u, 0u);
-            const double* dr = drive + (size_t)k * 10;
-            const float rf = (float)dr[0];
+            const float* dr = drive + (size_t)k * 10;
+            const float rf = __ldg(dr);
             const bool cube = reg == R_SPLIT || reg == R_COMBINE;
             float E[3], kick, u2v;
             {
@@ -342,7 +342,7 @@ __global__ void __launch_bounds__(128, 3) k_tm_step(TMConst C, MTracks M, uint32
                 if (cube) {   // fields.rs:89-96 clamps the grid coordinate to the grid
                     tx = __saturatef(tx); ty = __saturatef(ty); tz = __saturatef(tz);
                 }
-                const float ac = cube ? 0.0f : (float)dr[reg];
+                const float ac = cube ? 0.0f : __ldg(dr + reg);
 #pragma unroll
                 for (int d = 0; d < 3; ++d) {
                     float F[8];
@@ -724,7 +724,7 @@ cudaError_t store(State* s, const Tracks64& tr, uint32_t n, cudaStream_t st, uin
     return cudaGetLastError();
 }
 
-cudaError_t run(State* s, uint32_t n, const double* drive, uint64_t step0, uint64_t k, uint32_t* counts,
+cudaError_t run(State* s, uint32_t n, const float* drive, uint64_t step0, uint64_t k, uint32_t* counts,
                 unsigned long long* stepc, cudaStream_t st, uint32_t* launches) {
     cudaError_t e;
     if (!n) return cudaSuccess;
