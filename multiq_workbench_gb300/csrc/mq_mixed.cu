@@ -109,6 +109,7 @@ __device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& 
 struct Cell {
     float R[3][8], D[3][8], A[3][8];   // corner values per field and component, corner q = a + 2b + 4c
     int32_t ci, cj, ck;
+    float fci, fcj, fck;                // the same cell as floats (no int -> float conversion per step)
     uint32_t mask;                      // conductor bit per corner
 };
 
@@ -131,6 +132,7 @@ __device__ __forceinline__ void load_cell(const float4* __restrict__ nodes, cons
         if (q == 0) m = __float_as_uint(d.w);   // conductor bits of the cell's corners
     }
     c.ci = ci; c.cj = cj; c.ck = ck; c.mask = m;
+    c.fci = (float)ci; c.fcj = (float)cj; c.fck = (float)ck;
 }
 
 // pull the 4 corner runs of a cell into L1 ahead of use
@@ -193,6 +195,7 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
 #pragma unroll
     for (int d = 0; d < 3; ++d) { xh[d] = xl[d] = uh[d] = ul[d] = 0.f; }
     c.ci = c.cj = c.ck = -1; c.mask = 0;
+    c.fci = c.fcj = c.fck = __int_as_float(0x7fc00000);   // NaN: differs from every floored position
 
     for (;;) {
         // ---- refill: one warp-aggregated atomic hands out queue slots to lanes without an ion
@@ -268,9 +271,9 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
             // ---- field at the current position
             float tx = 0.f, ty = 0.f, tz = 0.f;
             if (!B.nearest) {
-                tx = __fadd_rn(__fsub_rn(xh[0], (float)c.ci), xl[0]);
-                ty = __fadd_rn(__fsub_rn(xh[1], (float)c.cj), xl[1]);
-                tz = __fadd_rn(__fsub_rn(xh[2], (float)c.ck), xl[2]);
+                tx = __fadd_rn(__fsub_rn(xh[0], c.fci), xl[0]);
+                ty = __fadd_rn(__fsub_rn(xh[1], c.fcj), xl[1]);
+                tz = __fadd_rn(__fsub_rn(xh[2], c.fck), xl[2]);
             }
             const float a_rf = B.v_rf * srf;
             const float a_ac = v_ac * sac;
@@ -366,14 +369,18 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
             }
             // ---- cell of the new position (refresh the cache before the conductor test), and
             //      an L1 prefetch of the cell one more step ahead
-            const int32_t fi = __float2int_rd(xh[0]), fj = __float2int_rd(xh[1]), fk = __float2int_rd(xh[2]);
-            const int32_t ci = clampi(fi, 0, B.nx - 2), cj = clampi(fj, 0, B.ny - 2), ck = clampi(fk, 0, B.nz - 2);
-            if (ci != c.ci || cj != c.cj || ck != c.ck) load_cell(nodes, B, ci, cj, ck, c);
+            // cell changes are found on floored floats; indices are formed only when one is seen
+            const float ffi = floorf(xh[0]), ffj = floorf(xh[1]), ffk = floorf(xh[2]);
+            if (ffi != c.fci || ffj != c.fcj || ffk != c.fck) {
+                const int32_t ci = clampi(__float2int_rd(xh[0]), 0, B.nx - 2), cj = clampi(__float2int_rd(xh[1]), 0, B.ny - 2),
+                              ck = clampi(__float2int_rd(xh[2]), 0, B.nz - 2);
+                if (ci != c.ci || cj != c.cj || ck != c.ck) load_cell(nodes, B, ci, cj, ck, c);
+            }
             if (PREFETCH) {
                 const int32_t pi = clampi(__float2int_rd(xh[0] + uh[0]), 0, B.nx - 2);
                 const int32_t pj = clampi(__float2int_rd(xh[1] + uh[1]), 0, B.ny - 2);
                 const int32_t pk = clampi(__float2int_rd(xh[2] + uh[2]), 0, B.nz - 2);
-                if (pi != ci || pj != cj || pk != ck) prefetch_cell(nodes, B, pi, pj, pk);
+                if (pi != c.ci || pj != c.cj || pk != c.ck) prefetch_cell(nodes, B, pi, pj, pk);
             }
             // ---- termination tests: exit, return, box, conductor, timeout
             // (a position exactly on a threshold is resolved by the high part alone; the box
@@ -381,13 +388,14 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
             int32_t status = 0;
             if (xh[2] > B.z_exit_h) status = 3;
             else if (xh[2] < B.z_ret_h) status = 2;
-            else if ((uint32_t)fi > (uint32_t)(B.nx - 2) || (uint32_t)fj > (uint32_t)(B.ny - 2) || (uint32_t)fk > (uint32_t)(B.nz - 2))
+            else if (ffi < 0.0f || ffj < 0.0f || ffk < 0.0f || ffi > B.lim_x - 1.0f || ffj > B.lim_y - 1.0f ||
+                     ffk > B.lim_z - 1.0f)
                 status = 4;
             else {
                 if (xh[2] > B.cz0_h && xh[2] < B.cz1_h) {
-                    const float fx = __fadd_rn(__fsub_rn(xh[0], (float)ci), xl[0]);
-                    const float fy = __fadd_rn(__fsub_rn(xh[1], (float)cj), xl[1]);
-                    const float fz = __fadd_rn(__fsub_rn(xh[2], (float)ck), xl[2]);
+                    const float fx = __fadd_rn(__fsub_rn(xh[0], c.fci), xl[0]);
+                    const float fy = __fadd_rn(__fsub_rn(xh[1], c.fcj), xl[1]);
+                    const float fz = __fadd_rn(__fsub_rn(xh[2], c.fck), xl[2]);
                     const uint32_t q = (fx >= 0.5f ? 1u : 0u) | (fy >= 0.5f ? 2u : 0u) | (fz >= 0.5f ? 4u : 0u);
                     if ((c.mask >> q) & 1u) status = 1;
                 }

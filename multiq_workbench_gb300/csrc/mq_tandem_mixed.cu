@@ -70,6 +70,8 @@ struct CubeF {   // cube geometry in mm, growth 0 (geometry.rs:136-205)
 struct PortM {
     const float4* rec;       // 48 B records: {RF.xyz, 0} {DC.xyz (+ gate bias), cell conductor bits} {AC.xyz, 0}
     int32_t nx, ny, nz, idle;
+    float lim[3];            // n - 1: the box of is_crash in grid units
+    float pad;
     float u2v, inv_h;        // h / dt [m/s per cell/step], 1 / h [1/m]
     float zret, zexit;       // Z_RETURN / h, Z_EXIT / h
     double h;                // [m]
@@ -174,6 +176,7 @@ __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? l
 struct TCell {
     float R[3][8], D[3][8], A[3][8];   // corner q = a + 2b + 4c
     int32_t ci, cj, ck, reg;
+    float fci, fcj, fck;                // the cell as floats (no int -> float conversion per step)
     uint32_t mask;                      // port: conductor bit per corner
 };
 
@@ -207,8 +210,10 @@ __device__ __forceinline__ void load_port(const PortM& P, int ci, int cj, int ck
     c.mask = m;
 }
 
-// the cell of grid position x (clamped to the grid), reloading the cache when it changes
+// the cell of grid position x (clamped to the grid), reloading the cache when it changes; a change
+// is found on floored floats, and indices are formed only when one is seen
 __device__ __forceinline__ void cell_for(const TMConst& C, int reg, const float xh[3], TCell& c) {
+    if (reg == c.reg && floorf(xh[0]) == c.fci && floorf(xh[1]) == c.fcj && floorf(xh[2]) == c.fck) return;
     const bool cube = reg == R_SPLIT || reg == R_COMBINE;
     const int nx = cube ? C.cn[0] : C.port[reg - 1].nx, ny = cube ? C.cn[1] : C.port[reg - 1].ny,
               nz = cube ? C.cn[2] : C.port[reg - 1].nz;
@@ -218,6 +223,7 @@ __device__ __forceinline__ void cell_for(const TMConst& C, int reg, const float 
         if (cube) load_cube(C.crec[reg == R_COMBINE ? 1 : 0], C.cn, ci, cj, ck, c);
         else load_port(C.port[reg - 1], ci, cj, ck, c);
         c.ci = ci; c.cj = cj; c.ck = ck; c.reg = reg;
+        c.fci = (float)ci; c.fcj = (float)cj; c.fck = (float)ck;
     }
 }
 
@@ -326,6 +332,7 @@ __global__ void __launch_bounds__(128, 3) k_tm_step(TMConst C, MTracks M, uint32
         TCell c;
         c.ci = c.cj = c.ck = -1;
         c.reg = -1;
+        c.fci = c.fcj = c.fck = __int_as_float(0x7fc00000);
         cell_for(C, reg, xh, c);
         uint4 rc = make_uint4(0, 0, 0, 0);
         for (uint32_t k = 0; k < S && reg <= R_COMBINE; ++k) {
@@ -336,9 +343,9 @@ __global__ void __launch_bounds__(128, 3) k_tm_step(TMConst C, MTracks M, uint32
             const bool cube = reg == R_SPLIT || reg == R_COMBINE;
             float E[3], kick, u2v;
             {
-                float tx = __fadd_rn(__fsub_rn(xh[0], (float)c.ci), xl[0]);
-                float ty = __fadd_rn(__fsub_rn(xh[1], (float)c.cj), xl[1]);
-                float tz = __fadd_rn(__fsub_rn(xh[2], (float)c.ck), xl[2]);
+                float tx = __fadd_rn(__fsub_rn(xh[0], c.fci), xl[0]);
+                float ty = __fadd_rn(__fsub_rn(xh[1], c.fcj), xl[1]);
+                float tz = __fadd_rn(__fsub_rn(xh[2], c.fck), xl[2]);
                 if (cube) {   // fields.rs:89-96 clamps the grid coordinate to the grid
                     tx = __saturatef(tx); ty = __saturatef(ty); tz = __saturatef(tz);
                 }
@@ -460,13 +467,13 @@ __global__ void __launch_bounds__(128, 3) k_tm_step(TMConst C, MTracks M, uint32
                 const PortM& P = C.port[i];
                 uint32_t* cnt = counts + (size_t)i * kNC;
                 // is_crash (world.rs:309-314): outside the box, or the nearest node is a conductor
-                bool crash = xh[0] < 0.0f || xh[1] < 0.0f || xh[2] < 0.0f || xh[0] > (float)(P.nx - 1) ||
-                             xh[1] > (float)(P.ny - 1) || xh[2] > (float)(P.nz - 1);
+                bool crash = xh[0] < 0.0f || xh[1] < 0.0f || xh[2] < 0.0f || xh[0] > P.lim[0] || xh[1] > P.lim[1] ||
+                             xh[2] > P.lim[2];
                 if (!crash) {
                     cell_for(C, reg, xh, c);
-                    const uint32_t qn = (__fadd_rn(__fsub_rn(xh[0], (float)c.ci), xl[0]) >= 0.5f ? 1u : 0u) |
-                                        (__fadd_rn(__fsub_rn(xh[1], (float)c.cj), xl[1]) >= 0.5f ? 2u : 0u) |
-                                        (__fadd_rn(__fsub_rn(xh[2], (float)c.ck), xl[2]) >= 0.5f ? 4u : 0u);
+                    const uint32_t qn = (__fadd_rn(__fsub_rn(xh[0], c.fci), xl[0]) >= 0.5f ? 1u : 0u) |
+                                        (__fadd_rn(__fsub_rn(xh[1], c.fcj), xl[1]) >= 0.5f ? 2u : 0u) |
+                                        (__fadd_rn(__fsub_rn(xh[2], c.fck), xl[2]) >= 0.5f ? 4u : 0u);
                     crash = (c.mask >> qn) & 1u;
                 }
                 if (crash) {
@@ -643,6 +650,7 @@ State* create(const mq_tandem_desc& d, const DevFields& f, cudaStream_t st, std:
         const mq_tandem_port& tp = d.port[i];
         PortM& P = C.port[i];
         P.nx = tp.dims[0]; P.ny = tp.dims[1]; P.nz = tp.dims[2];
+        for (int a = 0; a < 3; ++a) P.lim[a] = (float)(tp.dims[a] - 1);
         P.idle = tp.tone_khz == 0.0;
         P.h = tp.h;
         P.u2v = (float)(tp.h / d.dt);
