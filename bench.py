@@ -461,7 +461,7 @@ def main():
     (t_dev, t_wall), (steps_all,) = reduce_over_ranks([t_dev, t_wall], [steps_total], f"cuda:{local}")
     value = steps_all / t_dev
     e2e_value = steps_all / t_wall
-    counts = {k: int(sum(getattr(o, k) for o in out)) for k in ("transmitted", "returned", "crashed", "left", "timeout")}
+    counts = {k: int(getattr(out, k).sum()) for k in ("transmitted", "returned", "crashed", "left", "timeout")}
 
     extra = {}
     if rank == 0 and not args.no_f64:
@@ -474,9 +474,9 @@ def main():
         sm = eng.last_stats
         pulls = {}
         for k in ("transmitted", "returned", "crashed", "timeout"):
-            a = sum(getattr(o, k) for o in om)
-            b = sum(getattr(o, k) for o in o64)
-            n = sum(o.n for o in o64)
+            a = int(getattr(om, k).sum())
+            b = int(getattr(o64, k).sum())
+            n = int(o64.n.sum())
             p = (a + b + 1) / (2 * n + 2)
             pulls[k] = {"mixed": a, "fp64": b, "pull": (a - b) / math.sqrt(2 * n * p * (1 - p))}
         extra["fp64_gpu"] = {"value": s64.ion_steps / (s64.kernel_ms * 1e-3), "unit": UNIT,

@@ -3,12 +3,12 @@ filiprumenovski/multiq-workbench).  Public API mirrors chsim: ``Geom``, ``Fields
 ``Species``, ``RfAc``, ``Job``, ``Physics``, ``Outcome``, ``Engine.run_batch``; the tandem
 router mirrors trapsim: ``TandemModel``, ``CubeGeometry``, ``CubeFields``."""
 from .grid import Geom, Fields, cache_dir, cache_path
-from .channel import (Engine, Species, RfAc, Job, JobTable, Physics, Outcome, IonStates, RunStats, MqError, summarize, inject,
+from .channel import (Engine, Species, RfAc, Job, JobTable, Physics, Outcome, Outcomes, IonStates, RunStats, MqError, summarize, inject,
                       device_count, PREC_F64, PREC_MIXED, LAUNCH_DISC, LAUNCH_LEGACY, LAUNCH_GAUSSIAN, STATUS)
 from .tandem import (TandemModel, TandemPreset, TandemSpecies, CubeGeometry, CubeFields, PortGrid, Tracks, PortCounts,
                      Frame, TandemStats, DEFAULT_TONES)
 
-__all__ = ["Geom", "Fields", "cache_dir", "cache_path", "Engine", "Species", "RfAc", "Job", "JobTable", "Physics", "Outcome",
+__all__ = ["Geom", "Fields", "cache_dir", "cache_path", "Engine", "Species", "RfAc", "Job", "JobTable", "Physics", "Outcome", "Outcomes",
            "IonStates", "RunStats", "MqError", "summarize", "inject", "device_count", "PREC_F64", "PREC_MIXED", "LAUNCH_DISC",
            "LAUNCH_LEGACY", "LAUNCH_GAUSSIAN", "STATUS", "TandemModel", "TandemPreset", "TandemSpecies", "CubeGeometry",
            "CubeFields", "PortGrid", "Tracks", "PortCounts", "Frame", "TandemStats", "DEFAULT_TONES"]

@@ -10,6 +10,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+from collections.abc import Sequence
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -113,6 +114,49 @@ class Outcome:
     @classmethod
     def from_native(cls, o: N.mq_outcome) -> "Outcome":
         return cls(o.n, o.crashed, o.returned, o.transmitted, o.left, o.timeout, o.mean_coll, o.mean_time)
+
+
+OUTCOME_DTYPE = np.dtype([("n", "<u8"), ("crashed", "<u8"), ("returned", "<u8"), ("transmitted", "<u8"), ("left", "<u8"),
+                          ("timeout", "<u8"), ("mean_coll", "<f8"), ("mean_time", "<f8")])   # = mq_outcome
+
+
+class Outcomes(Sequence):
+    """Per-job outcomes (chsim's ``Vec<Outcome>``) held in one structured array filled by the
+    engine: indexing and iteration give ``Outcome`` objects, and a column name gives all jobs'
+    values at once (``outs.transmitted``), so no per-job object is built unless asked for."""
+
+    __slots__ = ("arr",)
+
+    def __init__(self, arr: np.ndarray):
+        self.arr = arr
+
+    @classmethod
+    def empty(cls, njobs: int) -> "Outcomes":
+        return cls(np.zeros(njobs, OUTCOME_DTYPE))
+
+    def ptr(self):
+        return self.arr.ctypes.data_as(C.POINTER(N.mq_outcome))
+
+    def __len__(self) -> int:
+        return len(self.arr)
+
+    def __getitem__(self, i):
+        if isinstance(i, slice):
+            return [self[k] for k in range(*i.indices(len(self)))]
+        r = self.arr[i]
+        return Outcome(int(r["n"]), int(r["crashed"]), int(r["returned"]), int(r["transmitted"]), int(r["left"]),
+                       int(r["timeout"]), float(r["mean_coll"]), float(r["mean_time"]))
+
+    def __getattr__(self, name):
+        if name in OUTCOME_DTYPE.names:
+            return self.arr[name]
+        raise AttributeError(name)
+
+    def __eq__(self, other) -> bool:
+        return list(self) == list(other)
+
+    def __repr__(self) -> str:
+        return f"Outcomes({len(self)} jobs)"
 
 
 ION_FIELDS = (("x", np.float64), ("y", np.float64), ("z", np.float64), ("vx", np.float64), ("vy", np.float64),
@@ -325,16 +369,16 @@ class Engine:
         self.last_stats = RunStats.from_native(st)
         return self.last_stats
 
-    def run_batch(self, jobs, dc, ph: Physics, ions_out: IonStates | None = None) -> list[Outcome]:
+    def run_batch(self, jobs, dc, ph: Physics, ions_out: IonStates | None = None) -> Outcomes:
         """Run many scan points in one batch; one Outcome per job (channel.rs:437-440)."""
-        out = (N.mq_outcome * len(jobs))()
+        out = Outcomes.empty(len(jobs))
         v = (C.c_double * 4)(*[float(x) for x in dc])
         st = N.mq_run_stats()
         io = C.byref(ions_out.native()) if ions_out is not None else None
-        N.check(N.lib().mq_run_batch(self._h, jobs_native(jobs), len(jobs), v, C.byref(ph.native()), out, io, C.byref(st)),
-                "mq_run_batch", self._h)
+        N.check(N.lib().mq_run_batch(self._h, jobs_native(jobs), len(jobs), v, C.byref(ph.native()), out.ptr(), io,
+                                     C.byref(st)), "mq_run_batch", self._h)
         self.last_stats = RunStats.from_native(st)
-        return [Outcome.from_native(o) for o in out]
+        return out
 
     def run_batch_ions(self, jobs, dc, ph: Physics) -> tuple[IonStates, np.ndarray]:
         """Final per-ion states and the job id of each ion (channel.rs:458-475)."""
@@ -355,9 +399,9 @@ def inject(fields: Fields, jobs, ph: Physics, pinned: bool = False) -> IonStates
     return ions
 
 
-def summarize(ions: IonStates, njobs: int, dt: float) -> list[Outcome]:
+def summarize(ions: IonStates, njobs: int, dt: float) -> Outcomes:
     """Per-job outcome counts (channel.rs:496-506)."""
-    out = (N.mq_outcome * njobs)()
+    out = Outcomes.empty(njobs)
     io = ions.native()
-    N.check(N.lib().mq_summarize(C.byref(io), len(ions), float(dt), njobs, out), "mq_summarize")
-    return [Outcome.from_native(o) for o in out]
+    N.check(N.lib().mq_summarize(C.byref(io), len(ions), float(dt), njobs, out.ptr()), "mq_summarize")
+    return out
