@@ -180,48 +180,68 @@ struct TCell {
     uint32_t mask;                      // port: conductor bit per corner
 };
 
-__device__ __forceinline__ void load_cube(const float4* __restrict__ rec, const int32_t cn[3], int ci, int cj, int ck,
-                                          TCell& c) {
-    const size_t sy = (size_t)cn[0], sz = (size_t)cn[0] * (size_t)cn[1];
-    const size_t base = (size_t)ci + sy * (size_t)cj + sz * (size_t)ck;
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-        const size_t o = 2 * (base + (size_t)(q & 1) + ((q & 2) ? sy : 0) + ((q & 4) ? sz : 0));
-        const float4 r = __ldg(rec + o), d = __ldg(rec + o + 1);
-        c.R[0][q] = r.x; c.R[1][q] = r.y; c.R[2][q] = r.z;
-        c.D[0][q] = d.x; c.D[1][q] = d.y; c.D[2][q] = d.z;
-    }
-    c.mask = 0;
-}
+// Constants of the track's current region, held in registers and refreshed only when the track
+// changes region (indexing the parameter block by region every step costs a slow indexed
+// constant load per access).
+struct RegK {
+    const float4* rec;            // node records of the region's grid
+    int32_t nx, ny, nz;
+    float kick, u2v;              // q/m dt^2 / h, h / dt
+    float lim0, lim1, lim2;       // port box n - 1 (grid units)
+    float zret, zexit;            // port return / exit planes (grid units)
+    bool cube, idle;
+};
 
-__device__ __forceinline__ void load_port(const PortM& P, int ci, int cj, int ck, TCell& c) {
-    const size_t sy = (size_t)P.nx, sz = (size_t)P.nx * (size_t)P.ny;
-    const size_t base = (size_t)ci + sy * (size_t)cj + sz * (size_t)ck;
-    uint32_t m = 0;
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-        const size_t o = 3 * (base + (size_t)(q & 1) + ((q & 2) ? sy : 0) + ((q & 4) ? sz : 0));
-        const float4 r = __ldg(P.rec + o), d = __ldg(P.rec + o + 1), a = __ldg(P.rec + o + 2);
-        c.R[0][q] = r.x; c.R[1][q] = r.y; c.R[2][q] = r.z;
-        c.D[0][q] = d.x; c.D[1][q] = d.y; c.D[2][q] = d.z;
-        c.A[0][q] = a.x; c.A[1][q] = a.y; c.A[2][q] = a.z;
-        if (q == 0) m = __float_as_uint(d.w);
+__device__ __forceinline__ void region_consts(const TMConst& C, int reg, float qmdt2, RegK& k) {
+    k.cube = reg == R_SPLIT || reg == R_COMBINE;
+    if (k.cube) {
+        k.rec = C.crec[reg == R_COMBINE ? 1 : 0];
+        k.nx = C.cn[0]; k.ny = C.cn[1]; k.nz = C.cn[2];
+        k.kick = qmdt2 * C.cinv_h;
+        k.u2v = C.cu2v;
+        k.idle = false;
+    } else {
+        const PortM& P = C.port[reg - 1];
+        k.rec = P.rec;
+        k.nx = P.nx; k.ny = P.ny; k.nz = P.nz;
+        k.kick = qmdt2 * P.inv_h;
+        k.u2v = P.u2v;
+        k.lim0 = P.lim[0]; k.lim1 = P.lim[1]; k.lim2 = P.lim[2];
+        k.zret = P.zret; k.zexit = P.zexit;
+        k.idle = P.idle != 0;
     }
-    c.mask = m;
 }
 
 // the cell of grid position x (clamped to the grid), reloading the cache when it changes; a change
 // is found on floored floats, and indices are formed only when one is seen
-__device__ __forceinline__ void cell_for(const TMConst& C, int reg, const float xh[3], TCell& c) {
+__device__ __forceinline__ void cell_for(const RegK& k, int reg, const float xh[3], TCell& c) {
     if (reg == c.reg && floorf(xh[0]) == c.fci && floorf(xh[1]) == c.fcj && floorf(xh[2]) == c.fck) return;
-    const bool cube = reg == R_SPLIT || reg == R_COMBINE;
-    const int nx = cube ? C.cn[0] : C.port[reg - 1].nx, ny = cube ? C.cn[1] : C.port[reg - 1].ny,
-              nz = cube ? C.cn[2] : C.port[reg - 1].nz;
-    const int ci = clampi(__float2int_rd(xh[0]), 0, nx - 2), cj = clampi(__float2int_rd(xh[1]), 0, ny - 2),
-              ck = clampi(__float2int_rd(xh[2]), 0, nz - 2);
+    const int ci = clampi(__float2int_rd(xh[0]), 0, k.nx - 2), cj = clampi(__float2int_rd(xh[1]), 0, k.ny - 2),
+              ck = clampi(__float2int_rd(xh[2]), 0, k.nz - 2);
     if (ci != c.ci || cj != c.cj || ck != c.ck || reg != c.reg) {
-        if (cube) load_cube(C.crec[reg == R_COMBINE ? 1 : 0], C.cn, ci, cj, ck, c);
-        else load_port(C.port[reg - 1], ci, cj, ck, c);
+        const size_t sy = (size_t)k.nx, sz = (size_t)k.nx * (size_t)k.ny;
+        const size_t base = (size_t)ci + sy * (size_t)cj + sz * (size_t)ck;
+        uint32_t m = 0;
+        if (k.cube) {
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const size_t o = 2 * (base + (size_t)(q & 1) + ((q & 2) ? sy : 0) + ((q & 4) ? sz : 0));
+                const float4 r = __ldg(k.rec + o), d = __ldg(k.rec + o + 1);
+                c.R[0][q] = r.x; c.R[1][q] = r.y; c.R[2][q] = r.z;
+                c.D[0][q] = d.x; c.D[1][q] = d.y; c.D[2][q] = d.z;
+            }
+        } else {
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const size_t o = 3 * (base + (size_t)(q & 1) + ((q & 2) ? sy : 0) + ((q & 4) ? sz : 0));
+                const float4 r = __ldg(k.rec + o), d = __ldg(k.rec + o + 1), a = __ldg(k.rec + o + 2);
+                c.R[0][q] = r.x; c.R[1][q] = r.y; c.R[2][q] = r.z;
+                c.D[0][q] = d.x; c.D[1][q] = d.y; c.D[2][q] = d.z;
+                c.A[0][q] = a.x; c.A[1][q] = a.y; c.A[2][q] = a.z;
+                if (q == 0) m = __float_as_uint(d.w);
+            }
+        }
+        c.mask = m;
         c.ci = ci; c.cj = cj; c.ck = ck; c.reg = reg;
         c.fci = (float)ci; c.fcj = (float)cj; c.fck = (float)ck;
     }
@@ -329,19 +349,22 @@ __global__ void __launch_bounds__(128, 3) k_tm_step(TMConst C, MTracks M, uint32
             uh[d] = M.uh[(size_t)d * n + id]; ul[d] = M.ul[(size_t)d * n + id];
         }
         const float qmdt2 = C.qmdt2[sp], nsd = C.nsd[sp], mr = C.mr[sp];
+        RegK rk;
+        region_consts(C, reg, qmdt2, rk);
         TCell c;
         c.ci = c.cj = c.ck = -1;
         c.reg = -1;
         c.fci = c.fcj = c.fck = __int_as_float(0x7fc00000);
-        cell_for(C, reg, xh, c);
+        cell_for(rk, reg, xh, c);
         uint4 rc = make_uint4(0, 0, 0, 0);
         for (uint32_t k = 0; k < S && reg <= R_COMBINE; ++k) {
             const uint64_t g = g0 + k;
             if (k == 0 || (g & 3) == 0) rc = philox(k0, k1, (uint32_t)(g >> 2), (uint32_t)(g >> 34), 0u, 0u);
             const float* dr = drive + (size_t)k * 10;
             const float rf = __ldg(dr);
-            const bool cube = reg == R_SPLIT || reg == R_COMBINE;
-            float E[3], kick, u2v;
+            const bool cube = rk.cube;
+            float E[3];
+            const float kick = rk.kick, u2v = rk.u2v;
             {
                 float tx = __fadd_rn(__fsub_rn(xh[0], c.fci), xl[0]);
                 float ty = __fadd_rn(__fsub_rn(xh[1], c.fcj), xl[1]);
@@ -358,17 +381,9 @@ __global__ void __launch_bounds__(128, 3) k_tm_step(TMConst C, MTracks M, uint32
                     E[d] = lerp3(F, tx, ty, tz);
                 }
             }
-            if (cube) {
-                kick = qmdt2 * C.cinv_h;
-                u2v = C.cu2v;
-                ++n_cube;
-            } else {
-                const PortM& P = C.port[reg - 1];
-                kick = qmdt2 * P.inv_h;
-                u2v = P.u2v;
-                if (P.idle) ++n_idle;
-                else ++n_port;
-            }
+            if (cube) ++n_cube;
+            else if (rk.idle) ++n_idle;
+            else ++n_port;
             // kick and drift, compensated (transport_step, lib.rs:90-103)
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
@@ -453,7 +468,8 @@ __global__ void __launch_bounds__(128, 3) k_tm_step(TMConst C, MTracks M, uint32
                             splitd(x[d] / h, xh[d], xl[d]);
                             splitd(v[d] * C.dt / h, uh[d], ul[d]);
                         }
-                        cell_for(C, reg, xh, c);
+                        region_consts(C, reg, qmdt2, rk);
+                        cell_for(rk, reg, xh, c);
                         continue;
                     }
                     if (p[2] > C.G.size) { reg = R_LOST; continue; }
@@ -461,16 +477,15 @@ __global__ void __launch_bounds__(128, 3) k_tm_step(TMConst C, MTracks M, uint32
                 if (p[1] > C.G.size && hypf2(p[0] - C.ent_c, p[2] - C.ent_b) >= C.G.ap_r) { reg = R_LOST; continue; }
                 if (p[1] > C.G.size + C.lext_mm) reg = reg == R_SPLIT ? 12 : 13;
                 else if (p[0] < 0.0f || p[1] < 0.0f || p[2] < 0.0f || p[0] > C.G.size) reg = R_LOST;
-                else cell_for(C, reg, xh, c);
+                else cell_for(rk, reg, xh, c);
             } else {
                 const int i = reg - 1;
-                const PortM& P = C.port[i];
                 uint32_t* cnt = counts + (size_t)i * kNC;
                 // is_crash (world.rs:309-314): outside the box, or the nearest node is a conductor
-                bool crash = xh[0] < 0.0f || xh[1] < 0.0f || xh[2] < 0.0f || xh[0] > P.lim[0] || xh[1] > P.lim[1] ||
-                             xh[2] > P.lim[2];
+                bool crash = xh[0] < 0.0f || xh[1] < 0.0f || xh[2] < 0.0f || xh[0] > rk.lim0 || xh[1] > rk.lim1 ||
+                             xh[2] > rk.lim2;
                 if (!crash) {
-                    cell_for(C, reg, xh, c);
+                    cell_for(rk, reg, xh, c);
                     const uint32_t qn = (__fadd_rn(__fsub_rn(xh[0], c.fci), xl[0]) >= 0.5f ? 1u : 0u) |
                                         (__fadd_rn(__fsub_rn(xh[1], c.fcj), xl[1]) >= 0.5f ? 2u : 0u) |
                                         (__fadd_rn(__fsub_rn(xh[2], c.fck), xl[2]) >= 0.5f ? 4u : 0u);
@@ -479,12 +494,13 @@ __global__ void __launch_bounds__(128, 3) k_tm_step(TMConst C, MTracks M, uint32
                 if (crash) {
                     reg = R_LOST;
                     atomicAdd(cnt + 15, 1u);
-                } else if (xh[2] < P.zret || xh[2] > P.zexit) {
+                } else if (xh[2] < rk.zret || xh[2] > rk.zexit) {
                     // leave (lib.rs:368-385) in FP64, then the cube's grid units
+                    const double h = C.port[i].h;
                     double x[3], v[3];
                     for (int d = 0; d < 3; ++d) {
-                        x[d] = ddv(xh[d], xl[d]) * P.h;
-                        v[d] = ddv(uh[d], ul[d]) * P.h / C.dt;
+                        x[d] = ddv(xh[d], xl[d]) * h;
+                        v[d] = ddv(uh[d], ul[d]) * h / C.dt;
                     }
                     x[0] += C.mouth_m[i][0] - C.axis_m;
                     x[1] += C.mouth_m[i][1] - C.axis_m;
@@ -505,7 +521,8 @@ __global__ void __launch_bounds__(128, 3) k_tm_step(TMConst C, MTracks M, uint32
                         splitd((x[d] * 1000.0 - C.clo_d[d]) / C.ch_d, xh[d], xl[d]);
                         splitd(v[d] * C.dt * 1000.0 / C.ch_d, uh[d], ul[d]);
                     }
-                    cell_for(C, reg, xh, c);
+                    region_consts(C, reg, qmdt2, rk);
+                    cell_for(rk, reg, xh, c);
                 }
             }
         }
