@@ -74,7 +74,8 @@ struct PortM {
     float pad;
     float u2v, inv_h;        // h / dt [m/s per cell/step], 1 / h [1/m]
     float zret, zexit;       // Z_RETURN / h, Z_EXIT / h
-    double h;                // [m]
+    double h, inv_hd;        // [m], 1 / h
+    double u2v_d, v2u_d;     // h / dt, dt / h (region changes convert with products, not divisions)
 };
 
 struct TMConst {
@@ -86,6 +87,7 @@ struct TMConst {
     float seam_mm, lext_mm, ent_b, ent_c;   // entrance axis centre: along z, along x [mm]
     float mouth_mm[9][2];
     double clo_d[3], ch_d, seam_m, axis_m, mouth_m[9][2];
+    double clo_m[3], ch_m, inv_ch_m, cu2v_d, cv2u_d;   // cube origin and spacing [m], 1 / h, h / dt, dt / h
     PortM port[9];
     float qmdt2[8], nsd[8], mr[8];   // per species: q/m dt^2 [m per V/m], n sigma dt, M/(m+M)
     float s_gas, pad1;
@@ -443,8 +445,8 @@ __global__ void __launch_bounds__(128, 3) k_tm_step(TMConst C, MTracks M, uint32
                         uint32_t* cnt = counts + (size_t)i * kNC;
                         double x[3], v[3];
                         for (int d = 0; d < 3; ++d) {
-                            x[d] = (C.clo_d[d] + ddv(xh[d], xl[d]) * C.ch_d) * 1e-3;
-                            v[d] = ddv(uh[d], ul[d]) * C.ch_d * 1e-3 / C.dt;
+                            x[d] = C.clo_m[d] + ddv(xh[d], xl[d]) * C.ch_m;
+                            v[d] = ddv(uh[d], ul[d]) * C.cu2v_d;
                         }
                         x[0] += C.axis_m - C.mouth_m[i][0];
                         x[1] += C.axis_m - C.mouth_m[i][1];
@@ -463,10 +465,10 @@ __global__ void __launch_bounds__(128, 3) k_tm_step(TMConst C, MTracks M, uint32
                             atomicAdd(cnt + 14, 1u);
                         }
                         reg = 1 + i;
-                        const double h = C.port[i].h;
+                        const double ih = C.port[i].inv_hd, v2u = C.port[i].v2u_d;
                         for (int d = 0; d < 3; ++d) {
-                            splitd(x[d] / h, xh[d], xl[d]);
-                            splitd(v[d] * C.dt / h, uh[d], ul[d]);
+                            splitd(x[d] * ih, xh[d], xl[d]);
+                            splitd(v[d] * v2u, uh[d], ul[d]);
                         }
                         region_consts(C, reg, qmdt2, rk);
                         cell_for(rk, reg, xh, c);
@@ -496,11 +498,11 @@ __global__ void __launch_bounds__(128, 3) k_tm_step(TMConst C, MTracks M, uint32
                     atomicAdd(cnt + 15, 1u);
                 } else if (xh[2] < rk.zret || xh[2] > rk.zexit) {
                     // leave (lib.rs:368-385) in FP64, then the cube's grid units
-                    const double h = C.port[i].h;
+                    const double h = C.port[i].h, u2v = C.port[i].u2v_d;
                     double x[3], v[3];
                     for (int d = 0; d < 3; ++d) {
                         x[d] = ddv(xh[d], xl[d]) * h;
-                        v[d] = ddv(uh[d], ul[d]) * h / C.dt;
+                        v[d] = ddv(uh[d], ul[d]) * u2v;
                     }
                     x[0] += C.mouth_m[i][0] - C.axis_m;
                     x[1] += C.mouth_m[i][1] - C.axis_m;
@@ -518,8 +520,8 @@ __global__ void __launch_bounds__(128, 3) k_tm_step(TMConst C, MTracks M, uint32
                         atomicAdd(cnt + 16 + sp, 1u);
                     }
                     for (int d = 0; d < 3; ++d) {
-                        splitd((x[d] * 1000.0 - C.clo_d[d]) / C.ch_d, xh[d], xl[d]);
-                        splitd(v[d] * C.dt * 1000.0 / C.ch_d, uh[d], ul[d]);
+                        splitd((x[d] - C.clo_m[d]) * C.inv_ch_m, xh[d], xl[d]);
+                        splitd(v[d] * C.cv2u_d, uh[d], ul[d]);
                     }
                     region_consts(C, reg, qmdt2, rk);
                     cell_for(rk, reg, xh, c);
@@ -635,6 +637,11 @@ State* create(const mq_tandem_desc& d, const DevFields& f, cudaStream_t st, std:
     }
     C.ch = (float)d.cube_h_mm;
     C.ch_d = d.cube_h_mm;
+    for (int a = 0; a < 3; ++a) C.clo_m[a] = d.cube_lo_mm[a] * 1e-3;
+    C.ch_m = d.cube_h_mm * 1e-3;
+    C.inv_ch_m = 1.0 / C.ch_m;
+    C.cu2v_d = C.ch_m / d.dt;
+    C.cv2u_d = d.dt / C.ch_m;
     C.cu2v = (float)(d.cube_h_mm * 1e-3 / d.dt);
     C.cinv_h = (float)(1.0 / (d.cube_h_mm * 1e-3));
     for (int r = 0; r < 2; ++r) {
@@ -670,6 +677,9 @@ State* create(const mq_tandem_desc& d, const DevFields& f, cudaStream_t st, std:
         for (int a = 0; a < 3; ++a) P.lim[a] = (float)(tp.dims[a] - 1);
         P.idle = tp.tone_khz == 0.0;
         P.h = tp.h;
+        P.inv_hd = 1.0 / tp.h;
+        P.u2v_d = tp.h / d.dt;
+        P.v2u_d = d.dt / tp.h;
         P.u2v = (float)(tp.h / d.dt);
         P.inv_h = (float)(1.0 / tp.h);
         P.zret = (float)(Z_RETURN / tp.h);
