@@ -231,6 +231,16 @@ def tandem_bytes(st, kind: str = "mixed") -> float:
     return b["cube"] * st.steps_cube + b["port"] * st.steps_port + b["idle"] * st.steps_idle
 
 
+def tandem_traffic():
+    """DRAM bytes of one full-size k_tm_step launch (256 steps) from the committed ncu summary."""
+    import re
+    prof = ROOT / "profiles" / "k_tm_step_tandem.md"
+    if not prof.exists():
+        return None
+    m = re.search(r"dram_bytes_per_launch:\s*([0-9.eE+]+)", prof.read_text())
+    return float(m.group(1)) if m else None
+
+
 def tandem_cpu(m, pulse, steps: int, target_s: float, threads: int) -> dict:
     """The tandem oracle on the first k tracks of the pulse for the same global steps, k grown
     until the run takes about ``target_s``."""
@@ -361,7 +371,7 @@ def run_tandem(args, rank: int, world: int):
                     "d2h_bytes_per_step": int(last.d2h_bytes)},
             "gpu_launches": int(sum(s.launches for s in sts)),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                         "traffic": None, "peak_source": "measured hbm_gbs" if peaks.get("hbm_gbs") else "fallback",
+                         "traffic": tandem_traffic(), "peak_source": "measured hbm_gbs" if peaks.get("hbm_gbs") else "fallback",
                          "kernel": "k_tm_step", "algorithmic_bytes_per_track_step": TANDEM_BYTES["mixed"]},
             "cpu_baseline": cpu, "clocks": clk,
             "census": {"split": f.split, "channel": f.channel, "combine": f.combine, "lost": f.lost, "back": f.back,
