@@ -12,6 +12,7 @@
 // thin plates and staircase electrodes without the Galerkin 27-point hierarchy the
 // reference builds (simulation/fieldsolve/src/mg.rs:1-40).
 #include "mq_grid.h"
+#include "mq_levels.h"
 #include "mq_pool.h"
 
 #include <chrono>
@@ -284,44 +285,40 @@ struct Solver {
     }
     void build_hierarchy(int nx, int ny, int nz, const uint8_t* fix0) {
         L.clear();
-        L.emplace_back();
-        Level& l0 = L.back();
-        l0.nx = nx; l0.ny = ny; l0.nz = nz;
-        l0.fix.assign(fix0, fix0 + l0.n());
-        l0.u.assign(l0.n(), 0.0); l0.rhs.assign(l0.n(), 0.0); l0.r.assign(l0.n(), 0.0);
-        for (;;) {
-            const Level& f = L.back();
-            int cx = f.nx / 2 + 1, cy = f.ny / 2 + 1, cz = f.nz / 2 + 1;
-            if (f.nx < 5 || f.ny < 5 || f.nz < 5 || cx < 3 || cy < 3 || cz < 3) break;
-            Level c;
-            c.nx = cx; c.ny = cy; c.nz = cz;
-            c.fix.assign(c.n(), 0);
-            for (int K = 0; K < cz; ++K)
-                for (int J = 0; J < cy; ++J)
-                    for (int I = 0; I < cx; ++I) {
-                        bool face = I == 0 || J == 0 || K == 0 || I == cx - 1 || J == cy - 1 || K == cz - 1;
-                        bool fx = face;
-                        if (!fx) {
-                            int i = 2 * I, j = 2 * J, k = 2 * K;
-                            fx = (i >= f.nx || j >= f.ny || k >= f.nz) ? true : f.fix[f.idx(i, j, k)] != 0;
-                        }
-                        c.fix[c.idx(I, J, K)] = fx ? 1 : 0;
-                    }
-            c.u.assign(c.n(), 0.0); c.rhs.assign(c.n(), 0.0); c.r.assign(c.n(), 0.0);
-            L.push_back(std::move(c));
+        const std::vector<mqlv::Dims> D = mqlv::hierarchy(nx, ny, nz);
+        for (size_t l = 0; l < D.size(); ++l) {
+            Level lv;
+            lv.nx = D[l].nx; lv.ny = D[l].ny; lv.nz = D[l].nz;
+            lv.fix.assign(lv.n(), 0);
+            if (l == 0) lv.fix.assign(fix0, fix0 + lv.n());
+            else mqlv::coarse_fix(D[l - 1], L.back().fix.data(), D[l], lv.fix.data());
+            lv.u.assign(lv.n(), 0.0); lv.rhs.assign(lv.n(), 0.0); lv.r.assign(lv.n(), 0.0);
+            L.push_back(std::move(lv));
         }
     }
 };
 
-// per-plane partial sums, combined in plane order (thread-count independent)
+// Sum of f(q) over the grid in a fixed order: each row in i order, the rows of a plane in j order,
+// the planes in k order (thread-count independent, and the order the device solver reproduces).
 template <class F>
-double plane_sum(mq::Pool& pool, int nz, F f) {
+double ordered_sum(mq::Pool& pool, int nx, int ny, int nz, F f) {
     std::vector<double> part(nz, 0.0);
-    pool.parallel_for(nz, [&](long k) { part[k] = f((int)k); });
+    pool.parallel_for(nz, [&](long k) {
+        double plane = 0.0;
+        for (int j = 0; j < ny; ++j) {
+            const size_t base = (size_t)nx * ((size_t)j + (size_t)ny * k);
+            double row = 0.0;
+            for (int i = 0; i < nx; ++i) row += f(base + i);
+            plane += row;
+        }
+        part[k] = plane;
+    });
     double s = 0.0;
     for (int k = 0; k < nz; ++k) s += part[k];
     return s;
 }
+
+// per-plane maxima, combined in plane order
 template <class F>
 double plane_max(mq::Pool& pool, int nz, F f) {
     std::vector<double> part(nz, 0.0);
@@ -434,12 +431,7 @@ mq_status mq_laplace_solve(int32_t nx, int32_t ny, int32_t nz, const uint8_t* ma
         S.vcycle(0);
     };
     auto dot = [&](const std::vector<double>& a, const std::vector<double>& b) {
-        return plane_sum(pool, nz, [&](int k) {
-            double s = 0.0;
-            size_t base = sz * k;
-            for (size_t q = base; q < base + sz; ++q) s += a[q] * b[q];
-            return s;
-        });
+        return ordered_sum(pool, nx, ny, nz, [&](size_t q) { return a[q] * b[q]; });
     };
 
     double rmax = true_residual();
@@ -453,18 +445,12 @@ mq_status mq_laplace_solve(int32_t nx, int32_t ny, int32_t nz, const uint8_t* ma
         double rz = dot(r, l0.u);
         int inner = 0;
         while (it < max_it) {
-            // q = S p (p vanishes at fixed nodes)
-            double pq = plane_sum(pool, nz, [&](int k) {
-                double s = 0.0;
-                for (int j = 0; j < ny; ++j)
-                    for (int i = 0; i < nx; ++i) {
-                        size_t q = (size_t)i + sy * j + sz * k;
-                        if (fix[q]) { qv[q] = 0.0; continue; }
-                        double nb = p[q - 1] + p[q + 1] + p[q - sy] + p[q + sy] + p[q - sz] + p[q + sz];
-                        qv[q] = 6.0 * p[q] - nb;
-                        s += p[q] * qv[q];
-                    }
-                return s;
+            // q = S p (p vanishes at fixed nodes), and p . q
+            double pq = ordered_sum(pool, nx, ny, nz, [&](size_t q) {
+                if (fix[q]) { qv[q] = 0.0; return 0.0; }
+                double nb = p[q - 1] + p[q + 1] + p[q - sy] + p[q + sy] + p[q - sz] + p[q + sz];
+                qv[q] = 6.0 * p[q] - nb;
+                return p[q] * qv[q];
             });
             if (!(pq > 0)) break;
             double alpha = rz / pq;
