@@ -14,8 +14,10 @@
  *   mq_geom_basis_problem         <- solve_basis's Problem::from_fn + basis_value
  *                                                                         simulation/chsim/src/channel.rs:111-120,143-151
  *   mq_laplace_solve              <- fieldsolve::solve                   simulation/fieldsolve/src/lib.rs:156-166
+ *   mq_laplace_solve_device       <- the same solve on the GPU (no counterpart in the reference, which solves on the CPU)
  *   mq_efield_central             <- chsim efield (central differences)  simulation/chsim/src/channel.rs:167-184
  *   mq_channel_basis              <- solve_basis + efield (+ RF mask)    simulation/chsim/src/channel.rs:143-165,204-217
+ *   mq_channel_basis_ex           <- the same with the solve on a chosen device
  *   mq_dc_combine                 <- Fields::dc_field                    simulation/chsim/src/channel.rs:219-226
  */
 #ifndef MQ_GRID_H
@@ -99,6 +101,10 @@ mq_status mq_geom_basis_problem(const mq_geom* g, int32_t basis, uint8_t* mask, 
 mq_status mq_laplace_solve(int32_t nx, int32_t ny, int32_t nz, const uint8_t* mask,
                            const double* fixed, double outer_bc, double tol, int32_t threads,
                            double* phi, mq_solve_stats* stats);
+/* mq_laplace_solve on CUDA device `device`: the same algorithm and the same floating-point
+ * operations in the same order, so the potential is bit-identical to the host solver's. */
+mq_status mq_laplace_solve_device(int32_t nx, int32_t ny, int32_t nz, const uint8_t* mask, const double* fixed,
+                                  double outer_bc, double tol, int32_t device, double* phi, mq_solve_stats* stats);
 
 /* E = -grad(phi) per node as float4 {Ex, Ey, Ez, 0}: central differences, one-sided at
  * the box faces.  h_m = spacing in metres. */
@@ -109,6 +115,9 @@ mq_status mq_efield_central(const double* phi, int32_t nx, int32_t ny, int32_t n
  * phi_out may be NULL. */
 mq_status mq_channel_basis(const mq_geom* g, int32_t basis, double tol, int32_t threads,
                            float* e4, double* phi_out, mq_solve_stats* stats);
+/* the same with the Laplace solve on CUDA device `device` (< 0: on the host) */
+mq_status mq_channel_basis_ex(const mq_geom* g, int32_t basis, double tol, int32_t threads, int32_t device,
+                              float* e4, double* phi_out, mq_solve_stats* stats);
 
 /* Combined static DC field out4[n] = sum_b (float)v[b] * dc4[b][n] in float, bases in
  * order 0..3 (a NULL basis contributes nothing). */

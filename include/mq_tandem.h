@@ -7,7 +7,7 @@
  *   mq_cube_classify                             <- Geometry::classify                    simulation/trapsim/src/geometry.rs:136-205
  *   mq_cube_size, mq_cube_port_axis, mq_cube_nearest_port
  *                                                <- size / port_axis_xy / nearest_port    simulation/trapsim/src/geometry.rs:74-125
- *   mq_cube_fields                               <- trapsim Fields::build                 simulation/trapsim/src/fields.rs:28-75
+ *   mq_cube_fields, mq_cube_fields_ex            <- trapsim Fields::build                 simulation/trapsim/src/fields.rs:28-75
  *   mq_cube_dc_combined                          <- Fields::dc_combined                   simulation/trapsim/src/fields.rs:76-86
  *   mq_efield_fieldsolve                         <- fieldsolve Solution::efield_f32       simulation/fieldsolve/src/field.rs:26-87
  *   mq_tandem_create / mq_tandem_destroy         <- trapsim::Model::new (fields, ports)   simulation/trapsim/src/lib.rs:106-175
@@ -58,6 +58,10 @@ mq_status mq_efield_fieldsolve(const double* phi, const uint8_t* mask, int32_t n
  * Call with all output pointers NULL to get dims[3] and lo_mm[3] first. */
 mq_status mq_cube_fields(const mq_cube_geom* g, double h_mm, double grow, double tol, int32_t threads, int32_t dims[3],
                          double lo_mm[3], float* rf4, float* wall4, float* ent4, float* ext4, mq_solve_stats stats[4]);
+/* the same with the Laplace solves on CUDA device `device` (< 0: on the host; same results) */
+mq_status mq_cube_fields_ex(const mq_cube_geom* g, double h_mm, double grow, double tol, int32_t threads, int32_t device,
+                            int32_t dims[3], double lo_mm[3], float* rf4, float* wall4, float* ent4, float* ext4,
+                            mq_solve_stats stats[4]);
 /* combined DC for post potential u0 (irrelevant to the force), wall, entrance and exit rods */
 mq_status mq_cube_dc_combined(size_t n, const float* wall4, const float* ent4, const float* ext4, double u0,
                               double uwall, double q_in, double q_out, float* out4);

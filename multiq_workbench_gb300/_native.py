@@ -187,6 +187,12 @@ def _declare(L) -> None:
     L.mq_efield_central.restype = C.c_int32
     L.mq_channel_basis.argtypes = [P(mq_geom), C.c_int32, C.c_double, C.c_int32, C.c_void_p, C.c_void_p, P(mq_solve_stats)]
     L.mq_channel_basis.restype = C.c_int32
+    L.mq_channel_basis_ex.argtypes = [P(mq_geom), C.c_int32, C.c_double, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
+                                      P(mq_solve_stats)]
+    L.mq_channel_basis_ex.restype = C.c_int32
+    L.mq_laplace_solve_device.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_double, C.c_double,
+                                          C.c_int32, C.c_void_p, P(mq_solve_stats)]
+    L.mq_laplace_solve_device.restype = C.c_int32
     L.mq_dc_combine.argtypes = [C.c_size_t, C.c_void_p * 4, P(C.c_double), C.c_void_p]
     L.mq_dc_combine.restype = C.c_int32
     if hasattr(L, "mq_engine_create"):
@@ -216,6 +222,10 @@ def _declare_tandem(L) -> None:
     L.mq_cube_fields.argtypes = [P(mq_cube_geom), C.c_double, C.c_double, C.c_double, C.c_int32, P(C.c_int32),
                                  P(C.c_double), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, P(mq_solve_stats)]
     L.mq_cube_fields.restype = C.c_int32
+    L.mq_cube_fields_ex.argtypes = [P(mq_cube_geom), C.c_double, C.c_double, C.c_double, C.c_int32, C.c_int32,
+                                    P(C.c_int32), P(C.c_double), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                    P(mq_solve_stats)]
+    L.mq_cube_fields_ex.restype = C.c_int32
     L.mq_cube_dc_combined.argtypes = [C.c_size_t, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double,
                                       C.c_double, C.c_double, C.c_void_p]
     L.mq_cube_dc_combined.restype = C.c_int32

@@ -2,7 +2,8 @@
 
 The host C++ is compiled with ``-ffp-contract=off`` so set-up arithmetic (grid solve,
 E field, injection constants) is bit-identical on x86-64 and aarch64 hosts; the FP64
-kernels (channel and tandem) are compiled with ``--fmad=false`` for the same reason.  Translation units are
+kernels (channel and tandem) and the device Laplace solver are compiled with ``--fmad=false``
+for the same reason.  Translation units are
 compiled in parallel; the whole build takes well under a minute.
 """
 from __future__ import annotations
@@ -30,6 +31,7 @@ CUDA_UNITS = [
     ("mq_mixed.cu", []),
     ("mq_tandem.cu", ["--fmad=false"]),
     ("mq_tandem_mixed.cu", []),
+    ("mq_solve.cu", ["--fmad=false"]),
     ("mq_noalloc.cu", []),
 ]
 CXX_UNITS = ["mq_grid.cpp", "mq_engine.cpp", "mq_cube.cpp"]

@@ -116,6 +116,12 @@ mq_status mq_efield_fieldsolve(const double* phi, const uint8_t* mask, int32_t n
 
 mq_status mq_cube_fields(const mq_cube_geom* g, double h_mm, double grow, double tol, int32_t threads, int32_t dims[3],
                          double lo_mm[3], float* rf4, float* wall4, float* ent4, float* ext4, mq_solve_stats stats[4]) {
+    return mq_cube_fields_ex(g, h_mm, grow, tol, threads, -1, dims, lo_mm, rf4, wall4, ent4, ext4, stats);
+}
+
+mq_status mq_cube_fields_ex(const mq_cube_geom* g, double h_mm, double grow, double tol, int32_t threads, int32_t device,
+                            int32_t dims[3], double lo_mm[3], float* rf4, float* wall4, float* ent4, float* ext4,
+                            mq_solve_stats stats[4]) {
     if (!g || !dims || !lo_mm || !(h_mm > 0)) return MQ_ERR_INVALID;
     double lo[3], hi[3];
     domain(*g, g->cap_gap + 1.0, lo, hi);   // fields.rs:29
@@ -162,7 +168,9 @@ mq_status mq_cube_fields(const mq_cube_geom* g, double h_mm, double grow, double
             fixed[q] = fx ? v : 0.0;
         }
         mq_solve_stats st;
-        mq_status s = mq_laplace_solve(n[0], n[1], n[2], mask.data(), fixed.data(), outer[b], tol, threads, phi.data(), &st);
+        mq_status s = device >= 0
+                          ? mq_laplace_solve_device(n[0], n[1], n[2], mask.data(), fixed.data(), outer[b], tol, device, phi.data(), &st)
+                          : mq_laplace_solve(n[0], n[1], n[2], mask.data(), fixed.data(), outer[b], tol, threads, phi.data(), &st);
         if (stats) stats[b] = st;
         if (s != MQ_OK) return s;   // assert!(st.converged), fields.rs:62
         s = mq_efield_fieldsolve(phi.data(), mask.data(), n[0], n[1], n[2], h_mm * 1e-3, outs[b]);

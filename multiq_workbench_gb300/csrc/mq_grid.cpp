@@ -515,6 +515,11 @@ mq_status mq_efield_central(const double* phi, int32_t nx, int32_t ny, int32_t n
 
 mq_status mq_channel_basis(const mq_geom* g, int32_t basis, double tol, int32_t threads,
                            float* e4, double* phi_out, mq_solve_stats* stats) {
+    return mq_channel_basis_ex(g, basis, tol, threads, -1, e4, phi_out, stats);
+}
+
+mq_status mq_channel_basis_ex(const mq_geom* g, int32_t basis, double tol, int32_t threads, int32_t device,
+                              float* e4, double* phi_out, mq_solve_stats* stats) {
     int32_t d[3];
     if (mq_geom_dims(g, d) != MQ_OK || !e4 || basis < 0 || basis > 5) return MQ_ERR_INVALID;
     size_t n = (size_t)d[0] * d[1] * d[2];
@@ -526,7 +531,8 @@ mq_status mq_channel_basis(const mq_geom* g, int32_t basis, double tol, int32_t 
     std::unique_ptr<double[]> own;
     double* phi = phi_out;
     if (!phi) { own.reset(new (std::nothrow) double[n]); phi = own.get(); if (!phi) return MQ_ERR_NOMEM; }
-    st = mq_laplace_solve(d[0], d[1], d[2], mask.data(), fixed.data(), outer, tol, threads, phi, stats);
+    st = device >= 0 ? mq_laplace_solve_device(d[0], d[1], d[2], mask.data(), fixed.data(), outer, tol, device, phi, stats)
+                     : mq_laplace_solve(d[0], d[1], d[2], mask.data(), fixed.data(), outer, tol, threads, phi, stats);
     if (st != MQ_OK) return st;
     st = mq_efield_central(phi, d[0], d[1], d[2], g->h_mm * 1e-3, e4);
     if (st != MQ_OK) return st;

@@ -171,9 +171,11 @@ class Fields:
         return self.nx * self.ny * self.nz
 
     @classmethod
-    def build(cls, geom: Geom, tol: float = 1e-7, bases=None, threads: int = 0, cache: bool = True) -> "Fields":
+    def build(cls, geom: Geom, tol: float = 1e-7, bases=None, threads: int = 0, cache: bool = True,
+              device: int | None = None) -> "Fields":
         """Solve (or load from the cache) the bases.  ``bases`` = indices to solve (default all
-        six); skipped DC bases are None and contribute nothing to ``dc_field``."""
+        six); skipped DC bases are None and contribute nothing to ``dc_field``.  ``device``: solve
+        on that CUDA device (bit-identical to the host solve) instead of the host."""
         nx, ny, nz = geom.dims()
         n = nx * ny * nz
         want = list(range(6)) if bases is None else sorted(set(int(b) for b in bases) | {0, 1})
@@ -198,8 +200,9 @@ class Fields:
                 info.append(SolveInfo(BASES[b], 0, float("nan"), 0.0, True))
             else:
                 st = N.mq_solve_stats()
-                N.check(L.mq_channel_basis(C.byref(gn), b, C.c_double(tol), int(threads), e4.ctypes.data, phi.ctypes.data,
-                                           C.byref(st)), f"solve {BASES[b]}")
+                N.check(L.mq_channel_basis_ex(C.byref(gn), b, C.c_double(tol), int(threads),
+                                              -1 if device is None else int(device), e4.ctypes.data, phi.ctypes.data,
+                                              C.byref(st)), f"solve {BASES[b]}")
                 info.append(SolveInfo(BASES[b], st.iterations, st.final_residual, st.seconds, False))
                 if cache:
                     try:

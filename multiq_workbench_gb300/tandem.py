@@ -179,7 +179,7 @@ class CubeFields:
 
     @classmethod
     def build(cls, geom: CubeGeometry, h_mm: float, grow: float = 0.4, tol: float = 1e-7, threads: int = 0,
-              cache: bool = True) -> "CubeFields":
+              cache: bool = True, device: int | None = None) -> "CubeFields":
         g = geom.native()
         dims, lo = (C.c_int32 * 3)(), (C.c_double * 3)()
         L = N.lib()
@@ -194,8 +194,9 @@ class CubeFields:
                 return cls(geom, h_mm, dims, lo, z["rf"], z["wall"], z["ent"], z["ext"])
         arrs = [np.zeros((n, 4), np.float32) for _ in range(4)]
         st = (N.mq_solve_stats * 4)()
-        N.check(L.mq_cube_fields(C.byref(g), float(h_mm), float(grow), float(tol), int(threads), dims, lo,
-                                 *[a.ctypes.data for a in arrs], st), "mq_cube_fields")
+        N.check(L.mq_cube_fields_ex(C.byref(g), float(h_mm), float(grow), float(tol), int(threads),
+                                    -1 if device is None else int(device), dims, lo, *[a.ctypes.data for a in arrs], st),
+                "mq_cube_fields")
         if cache:
             try:
                 path.parent.mkdir(parents=True, exist_ok=True)
