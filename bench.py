@@ -54,9 +54,112 @@ def workload(ions_per_job: int = 256, seed0: int = 0):
     return jobs, ph, [0.0, 5.0, -5.0, 0.0]
 
 
-def fields():
+def fields(device: int | None = None):
+    """The 0.100 mm channel grid (RF, AC, plate and downstream DC bases); ``device`` solves it on
+    the GPU (bit-identical to the host solve)."""
     import multiq_workbench_gb300 as mq
-    return mq.Fields.build(mq.Geom(), bases=[0, 1, 3, 4])
+    return mq.Fields.build(mq.Geom(), bases=[0, 1, 3, 4], device=device)
+
+
+GRID_METRIC = "ion-steps/s, 1 GB300: grid-resolution study, mixed precision vs plain FP64"
+GRID_SPACINGS = (0.1, 0.05, 0.1 / 3.0)
+
+
+def grid_workload(ions_per_job: int = 1000, njobs: int = 1024):
+    """The grid study's launch: 1,000 ions of m/z 499 (z = +1, N2 CCS 185.6 A^2), 100 V / 500 kHz RF,
+    0.5 V / 100 kHz excitation, replicated over 1,024 seeds; Gaussian sigma 0.1 mm at z = 1 mm,
+    300 K, 1 mTorr, dt 100 ns, <= 20,000 steps, legacy half-kick (the corrected update loses
+    every ion of this drive within a few RF periods)."""
+    import multiq_workbench_gb300 as mq
+    jobs = [mq.Job(mq.Species(499.0, 1.0, 185.6), mq.RfAc(100.0, 500e3, 0.5, 100e3), ions_per_job, seed)
+            for seed in range(njobs)]
+    ph = mq.Physics(legacy_force=True, pressure_pa=0.133322, temp_k=300.0, dt=1e-7, t_max=20000 * 1e-7,
+                    launch=mq.LAUNCH_GAUSSIAN, sigma_mm=0.1, z_inject_mm=1.0)
+    return jobs, ph, [0.0, 5.0, -5.0, 0.0]
+
+
+def run_gridstudy(args, rank: int, world: int):
+    """Config 3: the same launch on grids solved at 0.100, 0.050 and 0.0333 mm (on the GPU), the
+    mixed engine timed on each, the FP64 kernel run on the same ions for counts and per-ion
+    class agreement."""
+    import torch
+    import __graft_entry__ as ge
+    import multiq_workbench_gb300 as mq
+    ge.build()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    jobs, ph, dc = grid_workload(args.ions_per_job if args.ions_per_job != 256 else 1000)
+    table = mq.JobTable.from_jobs(jobs, pinned=True)
+    n = table.total_ions()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+    peaks = measured_peaks()
+    hbm = peaks.get("hbm_gbs") or 6800.0
+    grids = []
+    clocks = Clocks(local)
+    value = None
+    for h in GRID_SPACINGS:
+        t0 = time.perf_counter()
+        f = mq.Fields.build(mq.Geom.with_spacing(h), bases=[0, 1, 3, 4], cache=False, device=local)
+        t_solve = time.perf_counter() - t0
+        with mq.Engine(f, mq.PREC_MIXED, device=local) as eng:
+            for _ in range(args.warmup):
+                eng.run_batch(table, dc, ph)
+            if h == GRID_SPACINGS[-1]:
+                clocks.start()
+            ms, steps = [], 0
+            walls = []
+            for _ in range(args.steps):
+                flush_l2(flush)
+                torch.cuda.synchronize()
+                w0 = time.perf_counter()
+                eng.run_batch(table, dc, ph)
+                walls.append(time.perf_counter() - w0)
+                ms.append(eng.last_stats.kernel_ms)
+                steps = eng.last_stats.ion_steps
+            step_ms = eng.last_stats.step_kernel_ms
+            ions_m = mq.IonStates.empty(n)
+            om = eng.run_batch(table, dc, ph, ions_out=ions_m)
+        with mq.Engine(f, mq.PREC_F64, device=local) as e64:
+            ions_d = mq.IonStates.empty(n)
+            o64 = e64.run_batch(table, dc, ph, ions_out=ions_d)
+            s64 = e64.last_stats
+        rate = steps / (float(np.mean(ms)) * 1e-3)
+        cls = {k: (int(getattr(om, k).sum()), int(getattr(o64, k).sum())) for k in ("returned", "crashed", "left",
+                                                                                 "transmitted", "timeout")}
+        pulls = {}
+        for k, (a, b) in cls.items():
+            p = (a + b + 1) / (2 * n + 2)
+            pulls[k] = {"mixed": a, "fp64": b, "pull": (a - b) / math.sqrt(2 * n * p * (1 - p))}
+        nodes = f.nx * f.ny * f.nz
+        grids.append({"h_mm": h, "dims": [f.nx, f.ny, f.nz], "nodes": nodes,
+                      "node_records_gb": nodes * 48 / 1e9, "solve_s": t_solve,
+                      "mixed": {"value": rate, "unit": UNIT, "ms_per_step": float(np.mean(ms)),
+                                "e2e": steps / float(np.mean(walls)), "ion_steps": int(steps),
+                                "roofline_frac": BYTES_PER_ION_STEP * steps / (step_ms * 1e-3) / 1e9 / hbm},
+                      "fp64_gpu": {"value": s64.ion_steps / (s64.kernel_ms * 1e-3), "unit": UNIT},
+                      "counts": pulls,
+                      "class_agreement": float(np.mean(ions_m.status == ions_d.status))})
+        value = rate
+        del f
+    clk = clocks.stop()
+    if rank != 0:
+        return
+    fin = grids[-1]
+    line = {"metric": GRID_METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": fin["mixed"]["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+            "config": {"workload": f"grid study: {n:,} ions (1,000-ion m/z 499 launch x {len(jobs)} seeds), legacy "
+                                   "half-kick, grids solved on the GPU at 0.100 / 0.050 / 0.0333 mm; value = the "
+                                   "0.0333 mm grid", "l2_flush": "256 MB write before every timed step"},
+            "e2e": {"value": fin["mixed"]["e2e"], "unit": UNIT, "h2d_bytes_per_step": int(table.arr.nbytes),
+                    "d2h_bytes_per_step": int(len(jobs) * 64)},
+            "gpu_launches": None,
+            "roofline": {"bound": "hbm", "achieved": fin["mixed"]["roofline_frac"] * hbm, "peak": hbm, "unit": "GB/s",
+                         "frac": fin["mixed"]["roofline_frac"], "traffic": None,
+                         "peak_source": "measured hbm_gbs" if peaks.get("hbm_gbs") else "fallback",
+                         "kernel": "k_mixed", "algorithmic_bytes_per_ion_step": BYTES_PER_ION_STEP},
+            "cpu_baseline": None, "clocks": clk, "grids": grids}
+    print(json.dumps(line), flush=True)
 
 
 class Clocks:
@@ -396,8 +499,9 @@ def main():
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--ions-per-job", type=int, default=256,
                     help="ions per job (256 = the benchmark workload; smaller = a profiling case)")
-    ap.add_argument("--workload", default="sweep", choices=["sweep", "tandem"],
-                    help="sweep: the batched channel sweep (default); tandem: the nine-channel tandem transport")
+    ap.add_argument("--workload", default="sweep", choices=["sweep", "tandem", "gridstudy"],
+                    help="sweep: the batched channel sweep (default); tandem: the nine-channel tandem transport; "
+                         "gridstudy: one launch on grids solved at 0.100 / 0.050 / 0.0333 mm")
     ap.add_argument("--tracks", type=int, default=1 << 20, help="tandem: tracks in the pulse")
     ap.add_argument("--tandem-steps", type=int, default=1000, help="tandem: global steps per bench step")
     ap.add_argument("--port-h", type=float, default=0.05, help="tandem: port grid spacing [mm]")
@@ -412,6 +516,18 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl" if args.impl == "gb300" else "gloo")
+    if args.workload == "gridstudy":
+        if args.impl == "reference":
+            if rank == 0:
+                print(json.dumps({"impl": "reference", "metric": GRID_METRIC,
+                                  "unavailable": "the grid study's reference arm is the sweep's CPU port; run "
+                                                 "--impl reference without --workload for it"}), flush=True)
+        else:
+            run_gridstudy(args, rank, world)
+        if dist:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
     if args.workload == "tandem":
         run_tandem(args, rank, world)
         if dist:
