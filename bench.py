@@ -102,6 +102,9 @@ def run_gridstudy(args, rank: int, world: int):
         f = mq.Fields.build(mq.Geom.with_spacing(h), bases=[0, 1, 3, 4], cache=False, device=local)
         t_solve = time.perf_counter() - t0
         with mq.Engine(f, mq.PREC_MIXED, device=local) as eng:
+            tuned = None
+            if not args.no_tune:
+                tuned, _ = eng.autotune(jobs, dc, ph, sample_per_job=64)
             for _ in range(args.warmup):
                 eng.run_batch(table, dc, ph)
             if h == GRID_SPACINGS[-1]:
@@ -133,6 +136,7 @@ def run_gridstudy(args, rank: int, world: int):
         nodes = f.nx * f.ny * f.nz
         grids.append({"h_mm": h, "dims": [f.nx, f.ny, f.nz], "nodes": nodes,
                       "node_records_gb": nodes * 48 / 1e9, "solve_s": t_solve,
+                      "tuning": tuned,
                       "mixed": {"value": rate, "unit": UNIT, "ms_per_step": float(np.mean(ms)),
                                 "e2e": steps / float(np.mean(walls)), "ion_steps": int(steps),
                                 "roofline_frac": BYTES_PER_ION_STEP * steps / (step_ms * 1e-3) / 1e9 / hbm},
