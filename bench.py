@@ -102,9 +102,7 @@ def run_gridstudy(args, rank: int, world: int):
         f = mq.Fields.build(mq.Geom.with_spacing(h), bases=[0, 1, 3, 4], cache=False, device=local)
         t_solve = time.perf_counter() - t0
         with mq.Engine(f, mq.PREC_MIXED, device=local) as eng:
-            tuned = None
-            if not args.no_tune:
-                tuned, _ = eng.autotune(jobs, dc, ph, sample_per_job=64)
+            tuned = eng.tuning()   # the default launch shape (a sampled autotune picks worse ones here)
             for _ in range(args.warmup):
                 eng.run_batch(table, dc, ph)
             if h == GRID_SPACINGS[-1]:
