@@ -585,3 +585,140 @@ int mqr_summarize(const mqr_ions* io, size_t n, const mqr_batch* b, size_t njobs
     free(acc);
     return 0;
 }
+
+
+/* ------------------------------------------------------------------ independent form (validate.rs:49-94) */
+
+/* one field of the grid by a separate trilinear pass (world.rs:112-131, tri_one): weights
+   ((wx wy) wz) per corner, corners in i, j, k order */
+static void tri_one(const mqr_grid* g, const float* f4, const double x[3], double e[3]) {
+    const double gx = x[0] / g->h, gy = x[1] / g->h, gz = x[2] / g->h;
+    const size_t i = cell_lo(gx, g->nx), j = cell_lo(gy, g->ny), k = cell_lo(gz, g->nz);
+    const double tx = gx - (double)i, ty = gy - (double)j, tz = gz - (double)k;
+    e[0] = e[1] = e[2] = 0.0;
+    for (int di = 0; di < 2; ++di)
+        for (int dj = 0; dj < 2; ++dj)
+            for (int dk = 0; dk < 2; ++dk) {
+                const double wx = di ? tx : 1.0 - tx, wy = dj ? ty : 1.0 - ty, wz = dk ? tz : 1.0 - tz;
+                const size_t q = (i + di) + (size_t)g->nx * ((j + dj) + (size_t)g->ny * (k + dk));
+                for (int d = 0; d < 3; ++d) e[d] += wx * wy * wz * (double)f4[4 * q + d];
+            }
+}
+
+typedef struct {
+    const mqr_grid* g;
+    const mqr_indep* p;
+    uint64_t i0, i1;
+    mqr_counts c;
+} indep_job;
+
+static void* indep_worker(void* arg) {
+    indep_job* J = (indep_job*)arg;
+    const mqr_grid* g = J->g;
+    const mqr_indep* P = J->p;
+    const double m = P->mass * AMU, mg = 28.0 * AMU;
+    const double qm = P->z * QE / m, s_ion = sqrt(KB * 300.0 / m), mr = mg / (m + mg), sig = P->ccs_n2 * 1e-20;
+    const double ngas = P->pressure_pa / (KB * 300.0), s_gas = sqrt(KB * 300.0 / mg);
+    const double a = P->axis_mm * 1e-3, dt = P->dt;
+    const double lim[3] = {(double)(g->nx - 1) * g->h, (double)(g->ny - 1) * g->h, (double)(g->nz - 1) * g->h};
+    for (uint64_t id = J->i0; id < J->i1; ++id) {
+        uint64_t st = (id + 1) * 0x9E3779B97F4A7C15ull ^ P->seed;
+        const double r = 2.0e-3 * sqrt(xs_next(&st));
+        double sn, cs;
+        mqr_sincos2pi(xs_next(&st), &sn, &cs);
+        double x[3] = {a + r * cs, a + r * sn, 1.0e-3};
+        double u1 = xs_next(&st), u2 = xs_next(&st);
+        double v[3];
+        v[0] = s_ion * gs(u1, u2);
+        u1 = xs_next(&st); u2 = xs_next(&st);
+        v[1] = s_ion * gs(u1, u2);
+        u1 = xs_next(&st);
+        v[2] = s_ion * sqrt(-2.0 * mqr_log(u1 > 1e-300 ? u1 : 1e-300));
+        const double ph_ac = xs_next(&st);                  /* phases in turns */
+        double ph_rf = xs_next(&st);
+        if (P->rf_phase0) ph_rf = 0.0;
+        double t = 0.0;
+        uint64_t steps = 0;
+        int out = 5;
+        while (t < P->t_max) {
+            /* sin(2 pi (f t + phase)): this library's turn-based sine, own time accumulator */
+            double p = P->f_rf * t + ph_rf, s1, c1, s2, c2;
+            mqr_sincos2pi(p - floor(p), &s1, &c1);
+            p = P->f_ac * t + ph_ac;
+            mqr_sincos2pi(p - floor(p), &s2, &c2);
+            const double srf = s1 * P->v_rf, sac = s2 * P->v_ac;
+            double er[3], ea[3], ed[3];
+            tri_one(g, g->rf4, x, er);
+            tri_one(g, g->ac4, x, ea);
+            tri_one(g, g->dc4, x, ed);
+            for (int d = 0; d < 3; ++d) {
+                v[d] += qm * dt * (srf * er[d] + sac * ea[d] + ed[d]);
+                x[d] += v[d] * dt;
+            }
+            t += dt;
+            steps += 1;
+            const double vm = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+            const double bound = vm + 6.0 * s_gas;
+            if (xs_next(&st) < ngas * sig * dt * bound) {
+                double vg[3];
+                for (int d = 0; d < 3; ++d) {
+                    u1 = xs_next(&st);
+                    u2 = xs_next(&st);
+                    vg[d] = s_gas * gs(u1, u2);
+                }
+                const double gv[3] = {v[0] - vg[0], v[1] - vg[1], v[2] - vg[2]};
+                const double gl = sqrt(gv[0] * gv[0] + gv[1] * gv[1] + gv[2] * gv[2]);
+                if (xs_next(&st) * bound < gl) {
+                    const double c = 2.0 * xs_next(&st) - 1.0;
+                    double sp, cp;
+                    mqr_sincos2pi(xs_next(&st), &sp, &cp);
+                    const double omc = 1.0 - c * c;
+                    const double snn = sqrt(omc > 0.0 ? omc : 0.0);
+                    const double nn[3] = {snn * cp, snn * sp, c};
+                    for (int d = 0; d < 3; ++d) v[d] = v[d] - mr * gv[d] + mr * gl * nn[d];
+                }
+            }
+            if (x[2] > P->z_exit) { out = 3; break; }
+            if (x[2] < P->z_return) { out = 2; break; }
+            int crash = x[0] < 0.0 || x[1] < 0.0 || x[2] < 0.0 || x[0] > lim[0] || x[1] > lim[1] || x[2] > lim[2];
+            if (!crash) {
+                const size_t q = node_round(x[0] / g->h, g->nx) +
+                                 (size_t)g->nx * (node_round(x[1] / g->h, g->ny) + (size_t)g->ny * node_round(x[2] / g->h, g->nz));
+                crash = g->rf4[4 * q + 3] > 0.5f;
+            }
+            if (crash) { out = 1; break; }
+        }
+        J->c.steps += steps;
+        J->c.n += 1;
+        if (out == 3) J->c.transmitted += 1;
+        else if (out == 2) J->c.returned += 1;
+        else if (out == 1) J->c.crashed += 1;
+        else J->c.timeout += 1;
+    }
+    return NULL;
+}
+
+int mqr_run_independent(const mqr_grid* g, const mqr_indep* p, uint64_t n, int32_t threads, mqr_counts* out) {
+    if (!g || !p || !out || !(p->dt > 0)) return -1;
+    int nt = threads > 0 ? threads : nthreads_default();
+    if ((uint64_t)nt > n) nt = n ? (int)n : 1;
+    indep_job* jobs = (indep_job*)calloc((size_t)nt, sizeof(indep_job));
+    pthread_t* th = (pthread_t*)calloc((size_t)nt, sizeof(pthread_t));
+    if (!jobs || !th) { free(jobs); free(th); return -2; }
+    for (int t = 0; t < nt; ++t) {
+        jobs[t].g = g; jobs[t].p = p;
+        jobs[t].i0 = n * (uint64_t)t / (uint64_t)nt;
+        jobs[t].i1 = n * (uint64_t)(t + 1) / (uint64_t)nt;
+    }
+    for (int t = 1; t < nt; ++t) pthread_create(&th[t], NULL, indep_worker, &jobs[t]);
+    indep_worker(&jobs[0]);
+    for (int t = 1; t < nt; ++t) pthread_join(th[t], NULL);
+    memset(out, 0, sizeof(*out));
+    for (int t = 0; t < nt; ++t) {
+        out->n += jobs[t].c.n; out->transmitted += jobs[t].c.transmitted; out->crashed += jobs[t].c.crashed;
+        out->returned += jobs[t].c.returned; out->timeout += jobs[t].c.timeout; out->steps += jobs[t].c.steps;
+    }
+    free(jobs);
+    free(th);
+    return 0;
+}

@@ -12,6 +12,8 @@
  *   simulation/mqviz/src/world.rs:498-536   advance_with_field (kick, drift, collide, tests)
  *   simulation/mqviz/src/world.rs:538-549   advance_all (work split in chunks of 16 ions)
  *   simulation/mqviz/src/validate.rs:24-46  run_live seeding splitmix(seed + i*0x9E37)
+ *   simulation/mqviz/src/validate.rs:49-94  run_reference, the independent per-ion form
+ *   simulation/mqviz/src/world.rs:110-131   tri_one (one field per trilinear pass)
  * with chsim's physics switches restated in FP64:
  *   simulation/chsim/src/channel.rs:254-273  Physics (legacy / correct presets)
  *   simulation/chsim/src/channel.rs:342-381  inject (legacy point+cone launch, first free path)
@@ -103,6 +105,24 @@ int mqr_run_range(const mqr_grid* g, const mqr_batch* b, const mqr_job* jobs, si
                   uint64_t* steps_out);
 
 int mqr_summarize(const mqr_ions* ions, size_t n, const mqr_batch* b, size_t njobs, mqr_outcome* out);
+
+/* The independent per-ion form of validate.rs:49-94 (a cross-check of the table-driven integrator):
+ * own seeding ((id + 1) * golden ^ seed), own time accumulator t += dt, drive sin(2 pi (f t + phase))
+ * each step, a separate trilinear pass per field (world.rs:112-131), collisions inline, exit ->
+ * return -> crash tests, timeout at t_max.  Phases are drawn in turns (the reference draws radians,
+ * 2 pi u) and its sine is this library's turn-based one. */
+typedef struct mqr_indep {
+    double mass, z, ccs_n2;   /* Da, charge, N2 CCS [A^2]                 */
+    double v_rf, f_rf, v_ac, f_ac;
+    double pressure_pa, dt, t_max;
+    double axis_mm, z_exit, z_return;   /* [mm], [m], [m]               */
+    uint64_t seed;
+    int32_t rf_phase0, pad;
+} mqr_indep;
+
+typedef struct mqr_counts { uint64_t n, transmitted, crashed, returned, timeout, steps; } mqr_counts;
+
+int mqr_run_independent(const mqr_grid* g, const mqr_indep* p, uint64_t n, int32_t threads, mqr_counts* out);
 
 #ifdef __cplusplus
 }

@@ -46,6 +46,16 @@ class Outcome(C.Structure):
                 ("left", C.c_uint64), ("timeout", C.c_uint64), ("mean_coll", C.c_double), ("mean_time", C.c_double)]
 
 
+class Indep(C.Structure):
+    _fields_ = [(k, C.c_double) for k in ("mass", "z", "ccs_n2", "v_rf", "f_rf", "v_ac", "f_ac", "pressure_pa", "dt",
+                                          "t_max", "axis_mm", "z_exit", "z_return")] + \
+               [("seed", C.c_uint64), ("rf_phase0", C.c_int32), ("pad", C.c_int32)]
+
+
+class Counts(C.Structure):
+    _fields_ = [(k, C.c_uint64) for k in ("n", "transmitted", "crashed", "returned", "timeout", "steps")]
+
+
 FIELDS = (("x", np.float64), ("y", np.float64), ("z", np.float64), ("vx", np.float64), ("vy", np.float64),
           ("vz", np.float64), ("ph_rf", np.float64), ("ph_ac", np.float64), ("rng", np.uint64), ("steps", np.uint32),
           ("ncoll", np.uint32), ("leg", np.int32), ("status", np.int32), ("jid", np.uint32))
@@ -74,6 +84,8 @@ def lib():
         L.mqr_run_range.restype = C.c_int
         L.mqr_summarize.argtypes = [P(Ions), C.c_size_t, P(Batch), C.c_size_t, P(Outcome)]
         L.mqr_summarize.restype = C.c_int
+        L.mqr_run_independent.argtypes = [P(Grid), P(Indep), C.c_uint64, C.c_int32, P(Counts)]
+        L.mqr_run_independent.restype = C.c_int
         _lib = L
     return _lib
 
@@ -168,3 +180,17 @@ def summarize(s: State, b: Batch, njobs: int):
 
 def threads_default() -> int:
     return os.cpu_count() or 1
+
+
+def run_independent(g: Grid3, sp, v_rf: float, f_rf: float, v_ac: float, f_ac: float, pressure_pa: float, dt: float,
+                    t_max: float, axis_mm: float, z_exit: float, z_return: float, n: int, seed: int,
+                    rf_phase0: bool = True, threads: int = 0) -> dict:
+    """The independent per-ion form (simulation/mqviz/src/validate.rs:49-94) on a grid: counts of
+    transmitted / crashed / returned / timed-out ions and the steps taken."""
+    p = Indep(sp.mass, sp.z, sp.ccs_n2, v_rf, f_rf, v_ac, f_ac, pressure_pa, dt, t_max, axis_mm, z_exit, z_return,
+              int(seed) & (2 ** 64 - 1), int(bool(rf_phase0)), 0)
+    c = Counts()
+    if lib().mqr_run_independent(C.byref(g.g), C.byref(p), int(n), int(threads), C.byref(c)) != 0:
+        raise RuntimeError("mqr_run_independent failed")
+    return dict(n=c.n, transmitted=c.transmitted, crashed=c.crashed, returned=c.returned, timeout=c.timeout,
+                steps=c.steps)

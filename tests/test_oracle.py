@@ -85,3 +85,48 @@ def test_summarize_counts_and_means(built):
     assert (out[0]["crashed"], out[0]["returned"], out[0]["transmitted"]) == (1, 1, 1)
     assert (out[1]["left"], out[1]["timeout"], out[1]["n"]) == (1, 2, 3)   # status 0 counts as timeout (channel.rs:501)
     assert out[0]["mean_coll"] == 2.0 and math.isclose(out[1]["mean_time"], 50 * 1e-7)
+
+
+def _rows(c):
+    """Outcome fractions with binomial errors and T/(T+C), as simulation/mqviz/src/validate.rs:119-126 tabulates them."""
+    n = max(c["n"], 1)
+    out = {}
+    for k in ("transmitted", "crashed", "returned"):
+        p = c[k] / n
+        out[k] = (p, math.sqrt(p * (1 - p) / n))
+    m = max(c["transmitted"] + c["crashed"], 1)
+    p = c["transmitted"] / m
+    out["T/(T+C)"] = (p, math.sqrt(p * (1 - p) / m))
+    return out
+
+
+@pytest.mark.parametrize("rf0", [True, False])
+def test_independent_form_agrees_with_table_form(s14_coarse, rf0):
+    """The independent per-ion FP64 loop (validate.rs:49-94: own seeding, own time accumulator, a
+    trilinear pass per field, inline collisions) and the table-driven integrator give the same
+    outcome fractions within the reference's own bar, |pull| <= 2 on every row (validate.rs:128-135),
+    on the coarse S14 grid at an excited point with crashes, 8000 ions each, t_max 3 ms."""
+    import multiq_workbench_gb300 as mq
+    from oracle import mqref as R
+    f = s14_coarse
+    g = mq.Geom.s14(h_mm=0.4, n_xy=40)
+    lay = g.layers()
+    dc = [18.0, 24.0, 15.0, 20.0]
+    sp = mq.Species(499.0 * 5, 5.0, 2.95 * 499 ** (2 / 3) * 3)
+    G = R.Grid3(f.nx, f.ny, f.nz, f.h, f.rf, f.ac, f.dc_field(dc))
+    n, tmax = 8000, 3e-3
+    ind = R.run_independent(G, sp, 70.0, 500e3, 3.0, 84.25e3, 0.1, 4e-8, tmax, g.axis(), lay[4] * 1e-3, 0.5e-3, n,
+                            777, rf_phase0=rf0)
+    ph = mq.Physics(pressure_pa=0.1, dt=4e-8, t_max=tmax, launch=mq.LAUNCH_DISC, r_inject_mm=2.0, rf_phase0=rf0)
+    b = R.batch(ph, 70.0, 500e3, g.axis(), lay)
+    jobs = [mq.Job(sp, mq.RfAc(70.0, 500e3, 3.0, 84.25e3), n, 777)]
+    s = R.inject(b, jobs, n)
+    R.run(G, b, jobs, s)
+    o = R.summarize(s, b, 1)[0]
+    tab = dict(n=o["n"], transmitted=o["transmitted"], crashed=o["crashed"] + o["left"], returned=o["returned"])
+    assert ind["n"] == n and ind["crashed"] > 50 and ind["transmitted"] > 50
+    assert ind["transmitted"] + ind["crashed"] + ind["returned"] + ind["timeout"] == n
+    a, r = _rows(ind), _rows(tab)
+    for k in a:
+        pull = (a[k][0] - r[k][0]) / max(math.hypot(a[k][1], r[k][1]), 1e-300)
+        assert abs(pull) <= 2.0, (k, a[k], r[k], pull)
