@@ -2,11 +2,13 @@
 filiprumenovski/multiq-workbench).  Public API mirrors chsim: ``Geom``, ``Fields``,
 ``Species``, ``RfAc``, ``Job``, ``Physics``, ``Outcome``, ``Engine.run_batch``; the tandem
 router mirrors trapsim: ``TandemModel``, ``CubeGeometry``, ``CubeFields``; ``scan`` holds chsim's
-result cache and adaptive scan, ``check`` its batch self-check."""
+result cache and adaptive scan, ``check`` its batch self-check; ``sweep`` runs excitation-frequency
+sweeps of a species mixture as one batch and ``fit`` turns their counts into R = f0 / FWHM (mqviz
+``fit_sweep``)."""
 from .grid import Geom, Fields, cache_dir, cache_path
 from .channel import (Engine, Species, RfAc, Job, JobTable, Physics, Outcome, Outcomes, IonStates, RunStats, MqError, summarize, inject,
                       device_count, PREC_F64, PREC_MIXED, LAUNCH_DISC, LAUNCH_LEGACY, LAUNCH_GAUSSIAN, STATUS)
-from . import check, scan
+from . import check, scan, fit, sweep
 from .tandem import (TandemModel, TandemPreset, TandemSpecies, CubeGeometry, CubeFields, PortGrid, Tracks, PortCounts,
                      Frame, TandemStats, DEFAULT_TONES)
 

@@ -199,6 +199,49 @@ def _declare(L) -> None:
         _declare_engine(L)
     if hasattr(L, "mq_tandem_create"):
         _declare_tandem(L)
+    if hasattr(L, "mq_fit_binomial_curve"):
+        _declare_fit(L)
+
+
+class mq_res_fit(C.Structure):
+    _fields_ = [("shape", C.c_int32), ("converged", C.c_int32), ("p", C.c_double * 4), ("e", C.c_double * 4),
+                ("cov", C.c_double * 16), ("chi2", C.c_double), ("chi2_flat", C.c_double), ("dof", C.c_int64),
+                ("scale", C.c_double), ("n_pts", C.c_uint64), ("r", C.c_double), ("r_err", C.c_double),
+                ("has_boot", C.c_int32), ("pad", C.c_int32), ("r_boot_mean", C.c_double), ("r_boot_sd", C.c_double),
+                ("f0_boot_sd", C.c_double)]
+
+
+def _declare_fit(L) -> None:
+    P = C.POINTER
+    vp, sz, d, u64, i32 = C.c_void_p, C.c_size_t, C.c_double, C.c_uint64, C.c_int32
+    L.mq_fit_model.argtypes = [i32, vp, d]
+    L.mq_fit_model.restype = d
+    L.mq_fit_shape_sigma.argtypes = [i32, vp, vp, vp, sz, P(mq_res_fit)]
+    L.mq_fit_shape_sigma.restype = i32
+    L.mq_fit_binomial_shape.argtypes = [i32, vp, vp, vp, sz, u64, u64, P(mq_res_fit)]
+    L.mq_fit_binomial_shape.restype = i32
+    L.mq_fit_binomial_curve.argtypes = [vp, vp, vp, sz, u64, u64, P(mq_res_fit)]
+    L.mq_fit_binomial_curve.restype = i32
+    L.mq_fit_is_significant.argtypes = [P(mq_res_fit), vp, sz]
+    L.mq_fit_is_significant.restype = i32
+    L.mq_fit_r_mz.argtypes = [d, d, d, d, vp]
+    L.mq_fit_r_mz.restype = None
+    L.mq_rng_seed.argtypes = [u64]
+    L.mq_rng_seed.restype = u64
+    L.mq_rng_uniform.argtypes = [P(u64)]
+    L.mq_rng_uniform.restype = d
+    L.mq_rng_binomial_fill.argtypes = [P(u64), vp, vp, sz, vp]
+    L.mq_rng_binomial_fill.restype = None
+    L.mq_mathieu_beta.argtypes = [d, d]
+    L.mq_mathieu_beta.restype = d
+    L.mq_sec_freq_khz.argtypes = [d, d, d, d, d]
+    L.mq_sec_freq_khz.restype = d
+    L.mq_terrain_tables.argtypes = [i32, i32, i32, d, d, vp, vp * 4, sz, vp, vp, vp, P(sz)]
+    L.mq_terrain_tables.restype = i32
+    L.mq_terrain_compute.argtypes = [sz, sz, vp, vp, vp, vp, sz, d, vp, d, vp, vp]
+    L.mq_terrain_compute.restype = i32
+    L.mq_terrain_dfdmz.argtypes = [sz, sz, vp, vp, vp, d, d, d, vp, d]
+    L.mq_terrain_dfdmz.restype = d
 
 
 def _declare_tandem(L) -> None:

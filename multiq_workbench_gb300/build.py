@@ -34,7 +34,7 @@ CUDA_UNITS = [
     ("mq_solve.cu", ["--fmad=false"]),
     ("mq_noalloc.cu", []),
 ]
-CXX_UNITS = ["mq_grid.cpp", "mq_engine.cpp", "mq_cube.cpp"]
+CXX_UNITS = ["mq_grid.cpp", "mq_engine.cpp", "mq_cube.cpp", "mq_fit.cpp"]
 
 
 def _nvcc() -> str:
