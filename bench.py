@@ -94,6 +94,7 @@ def run_gridstudy(args, rank: int, world: int):
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
     peaks = measured_peaks()
     hbm = peaks.get("hbm_gbs") or 6800.0
+    l2 = l2_read_gbs(local)
     grids = []
     clocks = Clocks(local)
     value = None
@@ -120,27 +121,31 @@ def run_gridstudy(args, rank: int, world: int):
             step_ms = eng.last_stats.step_kernel_ms
             ions_m = mq.IonStates.empty(n)
             om = eng.run_batch(table, dc, ph, ions_out=ions_m)
-        with mq.Engine(f, mq.PREC_F64, device=local) as e64:
-            ions_d = mq.IonStates.empty(n)
-            o64 = e64.run_batch(table, dc, ph, ions_out=ions_d)
-            s64 = e64.last_stats
         rate = steps / (float(np.mean(ms)) * 1e-3)
-        cls = {k: (int(getattr(om, k).sum()), int(getattr(o64, k).sum())) for k in ("returned", "crashed", "left",
-                                                                                 "transmitted", "timeout")}
-        pulls = {}
-        for k, (a, b) in cls.items():
-            p = (a + b + 1) / (2 * n + 2)
-            pulls[k] = {"mixed": a, "fp64": b, "pull": (a - b) / math.sqrt(2 * n * p * (1 - p))}
+        pulls, s64, agree = {}, None, None
+        if not args.no_f64:
+            with mq.Engine(f, mq.PREC_F64, device=local) as e64:
+                ions_d = mq.IonStates.empty(n)
+                o64 = e64.run_batch(table, dc, ph, ions_out=ions_d)
+                s64 = e64.last_stats
+            cls = {k: (int(getattr(om, k).sum()), int(getattr(o64, k).sum())) for k in ("returned", "crashed", "left",
+                                                                                     "transmitted", "timeout")}
+            for k, (a, b) in cls.items():
+                p = (a + b + 1) / (2 * n + 2)
+                pulls[k] = {"mixed": a, "fp64": b, "pull": (a - b) / math.sqrt(2 * n * p * (1 - p))}
+            agree = float(np.mean(ions_m.status == ions_d.status))
         nodes = f.nx * f.ny * f.nz
         grids.append({"h_mm": h, "dims": [f.nx, f.ny, f.nz], "nodes": nodes,
                       "node_records_gb": nodes * 48 / 1e9, "solve_s": t_solve,
                       "tuning": tuned,
                       "mixed": {"value": rate, "unit": UNIT, "ms_per_step": float(np.mean(ms)),
                                 "e2e": steps / float(np.mean(walls)), "ion_steps": int(steps),
-                                "roofline_frac": BYTES_PER_ION_STEP * steps / (step_ms * 1e-3) / 1e9 / hbm},
-                      "fp64_gpu": {"value": s64.ion_steps / (s64.kernel_ms * 1e-3), "unit": UNIT},
+                                "roofline_frac": BYTES_PER_ION_STEP * steps / (step_ms * 1e-3) / 1e9 / hbm,
+                                "roofline_l2_frac": (BYTES_PER_ION_STEP * steps / (step_ms * 1e-3) / 1e9 / l2)
+                                if l2 else None},
+                      "fp64_gpu": {"value": s64.ion_steps / (s64.kernel_ms * 1e-3), "unit": UNIT} if s64 else None,
                       "counts": pulls,
-                      "class_agreement": float(np.mean(ions_m.status == ions_d.status))})
+                      "class_agreement": agree})
         value = rate
         del f
     clk = clocks.stop()
@@ -160,6 +165,9 @@ def run_gridstudy(args, rank: int, world: int):
                          "frac": fin["mixed"]["roofline_frac"], "traffic": None,
                          "peak_source": "measured hbm_gbs" if peaks.get("hbm_gbs") else "fallback",
                          "kernel": "k_mixed", "algorithmic_bytes_per_ion_step": BYTES_PER_ION_STEP},
+            "roofline_l2": {"achieved": fin["mixed"]["roofline_frac"] * hbm, "peak": l2, "unit": "GB/s",
+                            "frac": fin["mixed"]["roofline_l2_frac"],
+                            "peak_source": "L2 read bandwidth measured in this run (mq_measure_l2_read_gbs)"},
             "cpu_baseline": None, "clocks": clk, "grids": grids}
     print(json.dumps(line), flush=True)
 
@@ -266,6 +274,19 @@ def reduce_over_ranks(times, counts, device) -> tuple[list, list]:
 def rank_seed0(rank: int) -> int:
     """First job seed of a rank's replica of the workload (disjoint seed ranges per rank)."""
     return rank * 1_000_003
+
+
+def l2_read_gbs(device: int) -> float | None:
+    """L2 read bandwidth measured in this run (32 MiB resident buffer, 200 sweeps, L1 bypassed),
+    the denominator of the gather kernels' L2 roofline."""
+    import ctypes as C
+    from multiq_workbench_gb300 import _native as N
+    best = None
+    for _ in range(3):
+        g = C.c_double(0.0)
+        if N.lib().mq_measure_l2_read_gbs(int(device), 32 << 20, 200, C.byref(g)) == 0:
+            best = g.value if best is None else max(best, g.value)
+    return best
 
 
 def flush_l2(buf):
@@ -436,6 +457,7 @@ def run_tandem(args, rank: int, world: int):
         return
     peaks = measured_peaks()
     hbm = peaks.get("hbm_gbs") or 6800.0
+    l2 = l2_read_gbs(local)
     achieved = sum(tandem_bytes(s) for s in sts) / (sum(s.kernel_ms for s in sts) * 1e-3) / 1e9
     f = m.frame()
     cnt = m.counts_array()
@@ -478,6 +500,8 @@ def run_tandem(args, rank: int, world: int):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                          "traffic": tandem_traffic(), "peak_source": "measured hbm_gbs" if peaks.get("hbm_gbs") else "fallback",
                          "kernel": "k_tm_step", "algorithmic_bytes_per_track_step": TANDEM_BYTES["mixed"]},
+            "roofline_l2": {"achieved": achieved, "peak": l2, "unit": "GB/s", "frac": achieved / l2 if l2 else None,
+                            "peak_source": "L2 read bandwidth measured in this run (mq_measure_l2_read_gbs)"},
             "cpu_baseline": cpu, "clocks": clk,
             "census": {"split": f.split, "channel": f.channel, "combine": f.combine, "lost": f.lost, "back": f.back,
                        "detected": f.detected},
@@ -620,6 +644,7 @@ def main():
     peaks = measured_peaks()
     hbm = peaks.get("hbm_gbs")
     peak_src = "measured" if hbm else "fallback"
+    l2 = l2_read_gbs(local) if rank == 0 else None
     hbm = hbm or 6800.0
     kern_s = sum(step_ms) * 1e-3
     achieved = BYTES_PER_ION_STEP * steps_total / kern_s / 1e9
@@ -645,6 +670,10 @@ def main():
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                              "traffic": traffic, "peak_source": f"{peak_src} hbm_gbs",
                              "kernel": "k_mixed", "algorithmic_bytes_per_ion_step": BYTES_PER_ION_STEP},
+                "roofline_l2": {"achieved": achieved, "peak": l2, "unit": "GB/s",
+                                "frac": achieved / l2 if l2 else None,
+                                "peak_source": "L2 read bandwidth measured in this run (mq_measure_l2_read_gbs: "
+                                               "32 MiB resident, 200 sweeps, best of 3)"},
                 "cpu_baseline": cpu, "clocks": clk, "outcomes": counts}
         line.update(extra)
         print(json.dumps(line), flush=True)

@@ -95,6 +95,10 @@ typedef struct mq_run_stats {
 } mq_run_stats;
 
 int32_t     mq_device_count(void);
+/* Read bandwidth of the L2 cache on `device` [GB/s]: `passes` read sweeps (L1 bypassed) over a
+ * buffer of `bytes` (16 MiB..96 MiB, so it stays resident in L2), timed with CUDA events after one
+ * untimed sweep.  The denominator of the gather kernels' L2 roofline; no reference counterpart. */
+mq_status   mq_measure_l2_read_gbs(int32_t device, size_t bytes, int32_t passes, double* gbs);
 mq_status   mq_engine_create(const mq_grid_desc* grid, int32_t precision, int32_t device, mq_engine** out);
 void        mq_engine_destroy(mq_engine* e);
 const char* mq_last_error(mq_engine* e);

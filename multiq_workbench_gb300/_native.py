@@ -313,6 +313,8 @@ def _declare_engine(L) -> None:
     L.mq_summarize.restype = C.c_int32
     L.mq_device_count.argtypes = []
     L.mq_device_count.restype = C.c_int32
+    L.mq_measure_l2_read_gbs.argtypes = [C.c_int32, C.c_size_t, C.c_int32, P(C.c_double)]
+    L.mq_measure_l2_read_gbs.restype = C.c_int32
     L.mq_engine_get_tuning.argtypes = [C.c_void_p, P(mq_tuning)]
     L.mq_engine_get_tuning.restype = C.c_int32
     L.mq_engine_set_tuning.argtypes = [C.c_void_p, P(mq_tuning)]

@@ -33,6 +33,7 @@ CUDA_UNITS = [
     ("mq_tandem_mixed.cu", []),
     ("mq_solve.cu", ["--fmad=false"]),
     ("mq_noalloc.cu", []),
+    ("mq_probe.cu", []),
 ]
 CXX_UNITS = ["mq_grid.cpp", "mq_engine.cpp", "mq_cube.cpp", "mq_fit.cpp"]
 

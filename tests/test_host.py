@@ -101,3 +101,14 @@ def test_summarize_c_matches_oracle(built):
         assert (x.n, x.crashed, x.returned, x.transmitted, x.left, x.timeout) == \
                (y["n"], y["crashed"], y["returned"], y["transmitted"], y["left"], y["timeout"])
         assert x.mean_coll == y["mean_coll"] and x.mean_time == y["mean_time"]
+
+
+def test_l2_probe_refusals_without_device(built):
+    import ctypes as C
+    import multiq_workbench_gb300 as mq
+    from multiq_workbench_gb300 import _native as N
+    g = C.c_double(0.0)
+    assert N.lib().mq_measure_l2_read_gbs(0, 200 << 20, 10, C.byref(g)) == -1      # above 96 MiB
+    assert N.lib().mq_measure_l2_read_gbs(0, 32 << 20, 10, None) == -1
+    if mq.device_count() == 0:
+        assert N.lib().mq_measure_l2_read_gbs(0, 32 << 20, 10, C.byref(g)) == -6
