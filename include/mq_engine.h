@@ -135,6 +135,21 @@ mq_status   mq_engine_set_tuning(mq_engine* e, const mq_tuning* t);
 mq_status   mq_engine_autotune(mq_engine* e, const mq_job* jobs, size_t njobs, const double dc[4], const mq_physics* ph,
                                uint64_t sample_per_job, mq_tuning* best, double* best_rate);
 
+/* Host-side fault injection for tests of the error paths (the reference has none).  The next
+ * stepping call of the engine (mq_run_ions / mq_run_batch / mq_engine_autotune) fails once:
+ *   MQ_FAULT_LAUNCH_BUDGET  the launch sequence is cut to one launch of 16 steps, so live ions
+ *                           remain and the watchdog reports MQ_ERR_WATCHDOG from the real
+ *                           survivor count (mq_run_ions still writes the states back: the call
+ *                           resumes by calling again);
+ *   MQ_FAULT_ALLOC          MQ_ERR_NOMEM before any device allocation of the call;
+ *   MQ_FAULT_LAUNCH         MQ_ERR_CUDA in place of the first kernel launch.
+ * Nothing is faulted on the device; the engine stays usable.  MQ_FAULT_NONE clears. */
+#define MQ_FAULT_NONE          0
+#define MQ_FAULT_LAUNCH_BUDGET 1
+#define MQ_FAULT_ALLOC         2
+#define MQ_FAULT_LAUNCH        3
+mq_status   mq_engine_inject_fault(mq_engine* e, int32_t kind);
+
 /* ---------------------------------------------------------------------------------------
  * Allocation-free FP64 stepping (no counterpart in the reference).
  *

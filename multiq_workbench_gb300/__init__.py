@@ -7,12 +7,13 @@ sweeps of a species mixture as one batch and ``fit`` turns their counts into R =
 ``fit_sweep``)."""
 from .grid import Geom, Fields, cache_dir, cache_path
 from .channel import (Engine, Species, RfAc, Job, JobTable, Physics, Outcome, Outcomes, IonStates, RunStats, MqError, summarize, inject,
-                      device_count, PREC_F64, PREC_MIXED, LAUNCH_DISC, LAUNCH_LEGACY, LAUNCH_GAUSSIAN, STATUS)
+                      device_count, PREC_F64, PREC_MIXED, LAUNCH_DISC, LAUNCH_LEGACY, LAUNCH_GAUSSIAN, STATUS,
+                      FAULT_NONE, FAULT_LAUNCH_BUDGET, FAULT_ALLOC, FAULT_LAUNCH)
 from . import check, scan, fit, sweep
 from .tandem import (TandemModel, TandemPreset, TandemSpecies, CubeGeometry, CubeFields, PortGrid, Tracks, PortCounts,
                      Frame, TandemStats, DEFAULT_TONES)
 
 __all__ = ["Geom", "Fields", "cache_dir", "cache_path", "Engine", "Species", "RfAc", "Job", "JobTable", "Physics", "Outcome", "Outcomes",
            "IonStates", "RunStats", "MqError", "summarize", "inject", "device_count", "PREC_F64", "PREC_MIXED", "LAUNCH_DISC",
-           "LAUNCH_LEGACY", "LAUNCH_GAUSSIAN", "STATUS", "TandemModel", "TandemPreset", "TandemSpecies", "CubeGeometry",
+           "LAUNCH_LEGACY", "LAUNCH_GAUSSIAN", "STATUS", "FAULT_NONE", "FAULT_LAUNCH_BUDGET", "FAULT_ALLOC", "FAULT_LAUNCH", "TandemModel", "TandemPreset", "TandemSpecies", "CubeGeometry",
            "CubeFields", "PortGrid", "Tracks", "PortCounts", "Frame", "TandemStats", "DEFAULT_TONES"]

@@ -322,6 +322,8 @@ def _declare_engine(L) -> None:
     L.mq_engine_autotune.argtypes = [C.c_void_p, P(mq_job), C.c_size_t, P(C.c_double), P(mq_physics), C.c_uint64,
                                      P(mq_tuning), P(C.c_double)]
     L.mq_engine_autotune.restype = C.c_int32
+    L.mq_engine_inject_fault.argtypes = [C.c_void_p, C.c_int32]
+    L.mq_engine_inject_fault.restype = C.c_int32
     L.mq_run_ions_device_noalloc.argtypes = [P(mq_dev_grid), P(mq_job), C.c_size_t, P(mq_physics), P(mq_ions), C.c_size_t,
                                              C.c_uint32, C.c_void_p, P(C.c_uint64)]
     L.mq_run_ions_device_noalloc.restype = C.c_int32

@@ -23,6 +23,8 @@ MqError = N.MqError
 PREC_F64 = 0
 PREC_MIXED = 1
 LAUNCH_DISC, LAUNCH_LEGACY, LAUNCH_GAUSSIAN = 0, 1, 2
+# host-side fault injection (mq_engine_inject_fault): the engine's next stepping call fails once
+FAULT_NONE, FAULT_LAUNCH_BUDGET, FAULT_ALLOC, FAULT_LAUNCH = 0, 1, 2, 3
 STATUS = {0: "alive", 1: "crashed", 2: "returned", 3: "transmitted", 4: "left", 5: "timeout"}
 
 
@@ -345,6 +347,12 @@ class Engine:
         N.check(N.lib().mq_engine_autotune(self._h, jobs_native(jobs), len(jobs), v, C.byref(ph.native()),
                                            int(sample_per_job), C.byref(t), C.byref(rate)), "mq_engine_autotune", self._h)
         return self.tuning(), float(rate.value)
+
+    def inject_fault(self, kind: int) -> None:
+        """Make the next stepping call fail once, on the host (``FAULT_LAUNCH_BUDGET``: one 16-step
+        launch, then the watchdog; ``FAULT_ALLOC``: out of device memory; ``FAULT_LAUNCH``: a failed
+        kernel launch).  For tests of callers' error handling; nothing faults on the device."""
+        N.check(N.lib().mq_engine_inject_fault(self._h, int(kind)), "mq_engine_inject_fault", self._h)
 
     def set_dc(self, dc) -> None:
         v = (C.c_double * 4)(*[float(x) for x in dc])

@@ -73,6 +73,7 @@ struct mq_engine {
     HostBuf stage;                 // pinned staging: [job constants | job offsets | job seeds | counters]
     mqmix::Scratch mix;            // mixed-engine scratch (lists, queue counters, job table)
     mqmix::Tuning tune;            // launch shape of the mixed engine
+    int32_t fault = MQ_FAULT_NONE; // one-shot host-side fault for the next stepping call
 };
 
 namespace {
@@ -82,6 +83,7 @@ mq_status fail(mq_engine* e, mq_status code, const std::string& msg) {
     return code;
 }
 mq_status cuda_fail(mq_engine* e, cudaError_t c, const char* what) {
+    cudaGetLastError();   // clear a non-sticky error (failed allocation, bad launch shape) so later calls start clean
     std::string m = std::string(what) + ": " + cudaGetErrorString(c);
     return fail(e, c == cudaErrorMemoryAllocation ? MQ_ERR_NOMEM : MQ_ERR_CUDA, m);
 }
@@ -289,6 +291,15 @@ mqd::DevGrid dev_grid(const mq_engine* e) {
 // or the step budget is spent.  Each launch advances every live ion by <= kF64Chunk steps.
 mq_status run_f64(mq_engine* e, const Batch& b, uint32_t tlen, size_t n, uint32_t max_more, mq_run_stats* stats,
                   uint64_t* steps_out) {
+    const int32_t fault = e->fault;
+    e->fault = MQ_FAULT_NONE;
+    if (fault == MQ_FAULT_ALLOC) return fail(e, MQ_ERR_NOMEM, "FP64 engine: injected device allocation failure");
+    if (fault == MQ_FAULT_LAUNCH) return fail(e, MQ_ERR_CUDA, "FP64 engine: injected kernel launch failure");
+    // every ion times out at max_steps, so ceil(min(max_more, max_steps) / chunk) launches finish
+    // every ion; one more is allowed before the watchdog calls it
+    const uint64_t need = max_more < b.max_steps ? (uint64_t)max_more : (uint64_t)b.max_steps;
+    const uint64_t max_launches = fault == MQ_FAULT_LAUNCH_BUDGET ? 1 : (need + kF64Chunk - 1) / kF64Chunk + 1;
+    const uint32_t chunk = fault == MQ_FAULT_LAUNCH_BUDGET ? 16u : kF64Chunk;
     CK(e->misc.grow(64), "counters");
     unsigned long long* d_steps = e->misc.as<unsigned long long>();
     uint32_t* d_live = reinterpret_cast<uint32_t*>(d_steps + 1);
@@ -296,17 +307,17 @@ mq_status run_f64(mq_engine* e, const Batch& b, uint32_t tlen, size_t n, uint32_
     const double2* rf_tab = e->tabs.as<double2>();
     const double2* ac_tab = rf_tab + tlen;
     uint64_t budget = max_more;
-    uint32_t launches = 0;
+    uint32_t launches = 0, live = 0;
     float step_ms = 0.0f;
     for (;;) {
-        uint32_t L = budget < kF64Chunk ? (uint32_t)budget : kF64Chunk;
-        if (L == 0) break;
+        uint32_t L = budget < chunk ? (uint32_t)budget : chunk;
+        if (L == 0 || launches >= max_launches) break;
         CK(cudaMemsetAsync(d_live, 0, 4, e->st), "counter reset");
         CK(cudaEventRecord(e->ev[2], e->st), "event");
         CK(mqd::launch_f64_step(dev_grid(e), b, e->jobc.as<JobC>(), rf_tab, ac_tab, tlen, dev_ions(e), (uint32_t)n, L,
                                 d_steps, d_live, e->st), "FP64 step kernel");
         CK(cudaEventRecord(e->ev[3], e->st), "event");
-        uint32_t live = 0;
+        live = 0;
         CK(cudaMemcpyAsync(&live, d_live, 4, cudaMemcpyDeviceToHost, e->st), "live count");
         CK(cudaStreamSynchronize(e->st), "FP64 step kernel");
         float ms = 0.0f;
@@ -326,6 +337,8 @@ mq_status run_f64(mq_engine* e, const Batch& b, uint32_t tlen, size_t n, uint32_
         stats->step_kernel_launches += launches;
         stats->step_kernel_ms += step_ms;
     }
+    if (live != 0 && max_more >= b.max_steps)
+        return fail(e, MQ_ERR_WATCHDOG, "FP64 engine: launch budget exhausted with " + std::to_string(live) + " live ions");
     return MQ_OK;
 }
 
@@ -333,12 +346,23 @@ mq_status run_mixed(mq_engine* e, const mq_job* jobs, size_t njobs, const mq_phy
                     uint32_t max_more, mq_run_stats* stats, uint64_t* steps_out) {
     std::vector<mqmix::MixJob> mj(njobs);
     for (size_t k = 0; k < njobs; ++k) mj[k] = mqmix::make_mix_job(make_job(jobs[k], ph), b);
+    const int32_t fault = e->fault;
+    e->fault = MQ_FAULT_NONE;
+    if (fault == MQ_FAULT_ALLOC) return fail(e, MQ_ERR_NOMEM, "mixed engine: injected device allocation failure");
+    if (fault == MQ_FAULT_LAUNCH) return fail(e, MQ_ERR_CUDA, "mixed engine: injected kernel launch failure");
+    mqmix::Tuning tune = e->tune;
+    if (fault == MQ_FAULT_LAUNCH_BUDGET) {   // one launch of 16 steps
+        tune.max_launches = 1;
+        tune.chunk = 16;
+    }
     mqmix::RunInfo info;
-    cudaError_t c = mqmix::run(e->mix, e->tune, dev_grid(e), e->grid_gen, b, mj.data(), njobs, dev_ions(e), (uint32_t)n,
+    cudaError_t c = mqmix::run(e->mix, tune, dev_grid(e), e->grid_gen, b, mj.data(), njobs, dev_ions(e), (uint32_t)n,
                                max_more, e->st, &info);
     if (c != cudaSuccess) return cuda_fail(e, c, "mixed engine");
-    if (info.watchdog) return fail(e, MQ_ERR_WATCHDOG, "mixed engine: launch budget exhausted with live ions");
     *steps_out = info.ion_steps;
+    if (info.watchdog)
+        return fail(e, MQ_ERR_WATCHDOG, "mixed engine: launch budget exhausted with " + std::to_string(info.survivors) +
+                                            " live ions");
     if (stats) {
         stats->launches += info.graph_replays;
         stats->kernel_launches += info.kernel_launches;
@@ -392,10 +416,10 @@ mq_status mq_engine_create(const mq_grid_desc* g, int32_t precision, int32_t dev
     const float* src[6] = {g->rf4, g->ac4, g->dc4[0], g->dc4[1], g->dc4[2], g->dc4[3]};
     for (int k = 0; k < 6; ++k) {
         if (!src[k]) continue;
-        if (cudaMalloc((void**)dst[k], bytes) != cudaSuccess) return bail(MQ_ERR_NOMEM);
+        if (cudaMalloc((void**)dst[k], bytes) != cudaSuccess) { cudaGetLastError(); return bail(MQ_ERR_NOMEM); }
         if (cudaMemcpy(*dst[k], src[k], bytes, cudaMemcpyHostToDevice) != cudaSuccess) return bail(MQ_ERR_CUDA);
     }
-    if (cudaMalloc((void**)&e->d_dc, bytes) != cudaSuccess) return bail(MQ_ERR_NOMEM);
+    if (cudaMalloc((void**)&e->d_dc, bytes) != cudaSuccess) { cudaGetLastError(); return bail(MQ_ERR_NOMEM); }
     if (cudaMemset(e->d_dc, 0, bytes) != cudaSuccess) return bail(MQ_ERR_CUDA);
     e->tune = mqmix::default_tuning(device);
     *out = e;
@@ -489,6 +513,14 @@ mq_status mq_run_ions(mq_engine* e, const mq_job* jobs, size_t njobs, const mq_p
     uint64_t steps = 0;
     if (e->prec == MQ_PREC_F64) s = run_f64(e, b, tlen, n, max_more, stats, &steps);
     else s = run_mixed(e, jobs, njobs, *ph, b, n, max_more, stats, &steps);
+    if (s == MQ_ERR_WATCHDOG) {   // the states are the checkpoint: hand them back so the caller can resume
+        const std::string why = e->err;
+        mq_status s2 = copy_ions(e, io, n, false, &d2h);
+        if (s2 == MQ_OK && cudaStreamSynchronize(e->st) != cudaSuccess) s2 = MQ_ERR_CUDA;
+        if (s2 != MQ_OK) return s2;
+        e->err = why;
+        return s;
+    }
     if (s != MQ_OK) return s;
     if ((s = copy_ions(e, io, n, false, &d2h)) != MQ_OK) return s;
     CK(cudaEventRecord(e->ev[1], e->st), "event");
@@ -578,6 +610,13 @@ mq_status mq_engine_set_tuning(mq_engine* e, const mq_tuning* t) {
     e->tune.chunk = t->chunk;
     e->tune.use_graph = t->use_graph ? 1 : 0;
     e->tune.prefetch = t->prefetch ? 1 : 0;
+    return MQ_OK;
+}
+
+mq_status mq_engine_inject_fault(mq_engine* e, int32_t kind) {
+    if (!e) return MQ_ERR_INVALID;
+    if (kind < MQ_FAULT_NONE || kind > MQ_FAULT_LAUNCH) return fail(e, MQ_ERR_INVALID, "unknown fault kind");
+    e->fault = kind;
     return MQ_OK;
 }
 

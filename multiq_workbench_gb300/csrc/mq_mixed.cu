@@ -636,8 +636,9 @@ cudaError_t run(Scratch& s, const Tuning& t, DevGrid g, uint64_t grid_gen, const
     const uint64_t need = max_more < b.max_steps ? (uint64_t)max_more : (uint64_t)b.max_steps;
     if (need == 0) return cudaSuccess;
     const uint32_t chunk = t.chunk ? t.chunk : 4096;
-    const uint32_t launches = (uint32_t)((need + chunk - 1) / chunk);
-    const uint32_t last_chunk = (uint32_t)(need - (uint64_t)(launches - 1) * chunk);
+    const uint32_t full = (uint32_t)((need + chunk - 1) / chunk);
+    const uint32_t launches = (t.max_launches && t.max_launches < full) ? t.max_launches : full;
+    const uint32_t last_chunk = launches < full ? chunk : (uint32_t)(need - (uint64_t)(launches - 1) * chunk);
     // exact double-float state of re-queued ions (only when the call spans several launches)
     const size_t keep_bytes = launches > 1 ? (size_t)12 * n * sizeof(float) : 0;
     if (s.keep_cap < keep_bytes) {
@@ -691,6 +692,7 @@ cudaError_t run(Scratch& s, const Tuning& t, DevGrid g, uint64_t grid_gen, const
     info->kernel_launches += kernels;
     // after the last launch the surviving list must be empty unless the step budget ran out
     const uint32_t survivors = h.count[launches & 1];
+    info->survivors = survivors;
     info->watchdog = (survivors != 0 && max_more >= b.max_steps) ? 1 : 0;
     return cudaSuccess;
 }

@@ -43,6 +43,7 @@ struct Tuning {
     uint32_t chunk = 20000;    // steps per ion per launch (compaction interval)
     int use_graph = 1;         // replay the launch sequence as one CUDA graph
     int prefetch = 0;          // L1-prefetch the cell an ion is heading for
+    uint32_t max_launches = 0; // cap on launches per call (0 = as many as the step budget needs)
     int sms = 0;               // filled from the device
 };
 
@@ -70,6 +71,7 @@ struct RunInfo {
     uint32_t kernel_launches = 0;
     uint32_t graph_replays = 0;
     int watchdog = 0;
+    uint32_t survivors = 0;
 };
 
 MixJob make_mix_job(const mqp::JobC& j, const mqp::Batch& b);

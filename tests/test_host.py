@@ -112,3 +112,8 @@ def test_l2_probe_refusals_without_device(built):
     assert N.lib().mq_measure_l2_read_gbs(0, 32 << 20, 10, None) == -1
     if mq.device_count() == 0:
         assert N.lib().mq_measure_l2_read_gbs(0, 32 << 20, 10, C.byref(g)) == -6
+
+
+def test_fault_injection_needs_an_engine(built):
+    from multiq_workbench_gb300 import _native as N
+    assert N.lib().mq_engine_inject_fault(None, 1) == -1
