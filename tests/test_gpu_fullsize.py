@@ -1,0 +1,108 @@
+"""Parity at the full sizes of the measured workloads, through properties that do not depend on size
+(the oracle is too slow to replay these batches ion by ion):
+
+* the batched sweep (64 f_ac x 8 V_ac x 32 m/z x 256 ions = 4,194,304 ions on the 0.100 mm
+  grid): every ion finishes and is counted once; a rerun gives the same bits; every ion of
+  sampled jobs has the state it gets when its job runs alone; the mixed engine's outcome counts
+  match the FP64 kernel's (which is bit-exact with the oracle) within binomial limits;
+* the tandem (1,048,576 tracks, nine 0.050 mm port grids): the region census conserves tracks
+  at every frame, the port counters balance, and a rerun gives the same bits.
+"""
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _sweep_jobs(mq, ions_per_job=256):
+    fac = np.linspace(80e3, 120e3, 64)
+    vac = np.linspace(0.1, 1.0, 8)
+    mzs = [470.0 + 2 * k for k in range(32)]
+    jobs = []
+    for a in fac:
+        for v in vac:
+            for m in mzs:
+                jobs.append(mq.Job(mq.Species(m, 1.0, 2.95 * m ** (2.0 / 3.0)), mq.RfAc(100.0, 500e3, float(v), float(a)),
+                                   ions_per_job, len(jobs)))
+    ph = mq.Physics(legacy_force=True, pressure_pa=0.133322, temp_k=300.0, dt=1e-7, t_max=20000 * 1e-7,
+                    launch=mq.LAUNCH_GAUSSIAN, sigma_mm=0.1, z_inject_mm=1.0)
+    return jobs, ph, [0.0, 5.0, -5.0, 0.0]
+
+
+@pytest.fixture(scope="module")
+def grid_0p1(built):
+    import multiq_workbench_gb300 as mq
+    return mq.Fields.build(mq.Geom(), bases=[0, 1, 3, 4], cache=False, device=0)
+
+
+def test_full_sweep_properties(grid_0p1):
+    import multiq_workbench_gb300 as mq
+    from multiq_workbench_gb300 import check
+    jobs, ph, dc = _sweep_jobs(mq)
+    n = sum(j.n for j in jobs)
+    assert n == 4_194_304
+    with mq.Engine(grid_0p1, mq.PREC_MIXED) as e:
+        a = mq.IonStates.empty(n)
+        oa = e.run_batch(jobs, dc, ph, ions_out=a)
+        b = mq.IonStates.empty(n)
+        ob = e.run_batch(jobs, dc, ph, ions_out=b)
+        # every ion finishes, once, in its own job
+        assert np.all(a.status != 0) and np.all(oa.n == 256)
+        assert int(oa.crashed.sum() + oa.returned.sum() + oa.transmitted.sum() + oa.left.sum() + oa.timeout.sum()) == n
+        assert np.array_equal(a.jid, np.repeat(np.arange(len(jobs), dtype=np.uint32), 256))
+        # a rerun of the whole batch gives the same bits
+        assert oa == ob and check.compare(a, b)["differ"] == 0
+        # sampled jobs run alone give their ions the batch's states
+        for k in (0, 1, 4097, 8191, 12000, 16383):
+            alone, _ = e.run_batch_ions([jobs[k]], dc, ph)
+            part = mq.IonStates.empty(256)
+            for name, _ in mq.channel.ION_FIELDS:
+                getattr(part, name)[:] = getattr(a, name)[k * 256:(k + 1) * 256]
+            part.jid[:] = 0
+            assert check.compare(alone, part)["differ"] == 0, k
+        # mixed vs FP64 on 16 ions of every job
+        sj = [mq.Job(j.sp, j.drive, 16, j.seed) for j in jobs]
+        om = e.run_batch(sj, dc, ph)
+    with mq.Engine(grid_0p1, mq.PREC_F64) as e64:
+        o64 = e64.run_batch(sj, dc, ph)
+    m = int(o64.n.sum())
+    for k in ("transmitted", "returned", "crashed", "timeout"):
+        x, y = int(getattr(om, k).sum()), int(getattr(o64, k).sum())
+        p = (x + y + 1) / (2 * m + 2)
+        pull = (x - y) / math.sqrt(2 * m * p * (1 - p))
+        assert abs(pull) < 4.0, (k, x, y, pull)
+
+
+def test_full_tandem_properties(built):
+    import multiq_workbench_gb300 as mq
+    h = 0.05
+    ch = mq.Fields.build(mq.Geom.s14(h_mm=h, n_xy=int(round(16.0 / h))), cache=False, device=0)
+    pg = mq.PortGrid.from_fields(ch)
+    grids = [pg] + [pg.replica() for _ in range(8)]
+    n = 1 << 20
+    runs = []
+    for _ in range(2):
+        m = mq.TandemModel(mq.DEFAULT_TONES, n=n, seed=486, fine=True, mouth_start=True, port_grids=grids,
+                           precision=1, device=0)
+        fr = []
+        for _ in range(3):
+            m.advance(100)
+            f = m.frame()
+            fr.append(f)
+            assert f.split + f.channel + f.combine + f.lost + f.back + f.detected == n
+        cnt = m.counts_array()
+        # trapsim's routing identities (lib.rs:494-501): every entry into a port (forward or
+        # reverse) ends as a return, a forward or a loss, or is still inside a port
+        entered, returned, forwarded, lost_p, reverse = cnt[:, 0], cnt[:, 1], cnt[:, 2], cnt[:, 15], cnt[:, 14]
+        assert int((entered + reverse).sum()) == int((returned + forwarded + lost_p).sum()) + f.channel
+        assert cnt[:, 3].sum() == cnt[:, 5:14].sum() and cnt[:, 16:21].sum() == forwarded.sum()
+        assert (entered > 0).all()
+        runs.append((m.tracks.copy(), cnt.copy()))
+        m.close()
+    (ta, ca), (tb, cb) = runs
+    assert np.array_equal(ca, cb)
+    from multiq_workbench_gb300.tandem import TRACK_FIELDS
+    for k, _ in TRACK_FIELDS:
+        assert np.array_equal(getattr(ta, k).view(np.uint8), getattr(tb, k).view(np.uint8)), k
