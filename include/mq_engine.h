@@ -150,6 +150,17 @@ mq_status   mq_engine_autotune(mq_engine* e, const mq_job* jobs, size_t njobs, c
 #define MQ_FAULT_LAUNCH        3
 mq_status   mq_engine_inject_fault(mq_engine* e, int32_t kind);
 
+/* Bounds checks of the debug build (the library built with -DMQ_CHECK): every position-derived
+ * gather index and work-queue index of the stepping kernels is checked on the device, and an index
+ * out of range is replaced by 0 and recorded.  Reads (and with reset != 0 clears) the records of
+ * `device`: *enabled = 1 in a check build, 0 otherwise (then hits = 0); hits = out-of-range
+ * indices seen; site / index / limit describe the first.  mq_check_selftest passes one index equal
+ * to its limit through the check (no memory access), so a check build must then report a hit at
+ * site 99. */
+mq_status   mq_check_status(int32_t device, int32_t reset, int32_t* enabled, uint32_t* hits, uint32_t* site,
+                            uint64_t* index, uint64_t* limit);
+mq_status   mq_check_selftest(int32_t device);
+
 /* ---------------------------------------------------------------------------------------
  * Allocation-free FP64 stepping (no counterpart in the reference).
  *

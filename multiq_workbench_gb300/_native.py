@@ -7,9 +7,11 @@ loudly if it is missing: there is no Python or CPU fallback for any engine call.
 from __future__ import annotations
 
 import ctypes as C
+import os
 from pathlib import Path
 
-_LIB_PATH = Path(__file__).resolve().parent / "libmqgb.so"
+# MQ_LIB selects another build of the library (the bounds-checked libmqgb_check.so)
+_LIB_PATH = Path(os.environ["MQ_LIB"]) if os.environ.get("MQ_LIB") else Path(__file__).resolve().parent / "libmqgb.so"
 _lib = None
 
 MQ_OK = 0
@@ -324,6 +326,11 @@ def _declare_engine(L) -> None:
     L.mq_engine_autotune.restype = C.c_int32
     L.mq_engine_inject_fault.argtypes = [C.c_void_p, C.c_int32]
     L.mq_engine_inject_fault.restype = C.c_int32
+    L.mq_check_status.argtypes = [C.c_int32, C.c_int32, P(C.c_int32), P(C.c_uint32), P(C.c_uint32), P(C.c_uint64),
+                                  P(C.c_uint64)]
+    L.mq_check_status.restype = C.c_int32
+    L.mq_check_selftest.argtypes = [C.c_int32]
+    L.mq_check_selftest.restype = C.c_int32
     L.mq_run_ions_device_noalloc.argtypes = [P(mq_dev_grid), P(mq_job), C.c_size_t, P(mq_physics), P(mq_ions), C.c_size_t,
                                              C.c_uint32, C.c_void_p, P(C.c_uint64)]
     L.mq_run_ions_device_noalloc.restype = C.c_int32

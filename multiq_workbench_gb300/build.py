@@ -21,6 +21,8 @@ CSRC = PKG / "csrc"
 INCLUDE = ROOT / "include"
 BUILD = PKG / "_build"
 LIB = PKG / "libmqgb.so"
+CHECK_BUILD = PKG / "_build_check"
+CHECK_LIB = PKG / "libmqgb_check.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CXXFLAGS = ["-O3", "-std=c++17", "-fPIC", "-pthread", "-ffp-contract=off", "-Wall", "-Wno-unused-function"]
@@ -59,39 +61,44 @@ def _stale(obj: Path, src: Path) -> bool:
     return any(d.stat().st_mtime > t for d in deps if d.exists())
 
 
-def build(verbose: bool = False, force: bool = False) -> Path:
+def build(verbose: bool = False, force: bool = False, check: bool = False) -> Path:
+    """Compile the library; ``check=True`` makes the bounds-checked debug build
+    ``libmqgb_check.so`` (-DMQ_CHECK, its own object directory) instead."""
     nvcc = _nvcc()
-    BUILD.mkdir(exist_ok=True)
+    bdir, lib = (CHECK_BUILD, CHECK_LIB) if check else (BUILD, LIB)
+    defs = ["-DMQ_CHECK"] if check else []
+    bdir.mkdir(exist_ok=True)
     jobs = []
     objs = []
     for name, extra in CUDA_UNITS:
         src = CSRC / name
         if not src.exists():
             continue
-        obj = BUILD / (name + ".o")
+        obj = bdir / (name + ".o")
         objs.append(obj)
         if force or _stale(obj, src):
             jobs.append([nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
-                         "-Xptxas", "-warn-spills", *extra, f"-I{INCLUDE}", f"-I{CSRC}", "-c", str(src), "-o", str(obj)])
+                         "-Xptxas", "-warn-spills", *defs, *extra, f"-I{INCLUDE}", f"-I{CSRC}", "-c", str(src), "-o", str(obj)])
     for name in CXX_UNITS:
         src = CSRC / name
         if not src.exists():
             continue
-        obj = BUILD / (name + ".o")
+        obj = bdir / (name + ".o")
         objs.append(obj)
         if force or _stale(obj, src):
-            jobs.append(["g++", *CXXFLAGS, f"-I{INCLUDE}", f"-I{CSRC}", "-I/usr/local/cuda/include", "-c", str(src), "-o", str(obj)])
+            jobs.append(["g++", *CXXFLAGS, *defs, f"-I{INCLUDE}", f"-I{CSRC}", "-I/usr/local/cuda/include", "-c", str(src),
+                         "-o", str(obj)])
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         for cmd, fut in [(c, ex.submit(_run, c)) for c in jobs]:
             if verbose:
                 print(" ".join(cmd), file=sys.stderr)
             fut.result()
-    if jobs or not LIB.exists():
-        tmp = LIB.with_suffix(".so.tmp")
+    if jobs or not lib.exists():
+        tmp = lib.with_suffix(".so.tmp")
         _run([nvcc, *ARCH, "-shared", "-cudart", "static", "-o", str(tmp), *map(str, objs), "-lpthread", "-ldl", "-lrt"])
-        os.replace(tmp, LIB)
-    return LIB
+        os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":
-    print(build(verbose=True, force="--force" in sys.argv))
+    print(build(verbose=True, force="--force" in sys.argv, check="--check" in sys.argv))

@@ -620,6 +620,51 @@ mq_status mq_engine_inject_fault(mq_engine* e, int32_t kind) {
     return MQ_OK;
 }
 
+}  // extern "C" (reopened below)
+
+struct MqCheckWordC { unsigned int hits, site; unsigned long long index, limit; };
+extern "C" int mq_check_read_f64(MqCheckWordC*, int);
+extern "C" int mq_check_read_mixed(MqCheckWordC*, int);
+extern "C" int mq_check_read_tandem(MqCheckWordC*, int);
+extern "C" int mq_check_read_tandem_mixed(MqCheckWordC*, int);
+extern "C" int mq_check_read_probe(MqCheckWordC*, int);
+extern "C" int mq_check_selftest_launch(void);
+
+extern "C" {
+
+mq_status mq_check_status(int32_t device, int32_t reset, int32_t* enabled, uint32_t* hits, uint32_t* site,
+                          uint64_t* index, uint64_t* limit) {
+    if (!enabled || !hits || !site || !index || !limit) return MQ_ERR_INVALID;
+    if (mq_device_count() <= device || device < 0) return MQ_ERR_NO_DEVICE;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    if (cudaSetDevice(device) != cudaSuccess) { cudaGetLastError(); return MQ_ERR_CUDA; }
+    int (*readers[])(MqCheckWordC*, int) = {mq_check_read_f64, mq_check_read_mixed, mq_check_read_tandem,
+                                            mq_check_read_tandem_mixed, mq_check_read_probe};
+    *enabled = 0; *hits = 0; *site = 0; *index = 0; *limit = 0;
+    mq_status st = MQ_OK;
+    for (auto rd : readers) {
+        MqCheckWordC w;
+        const int r = rd(&w, reset);
+        if (r < 0) { st = MQ_ERR_CUDA; break; }
+        if (r == 0) *enabled = 1;
+        if (w.hits && *hits == 0) { *site = w.site; *index = w.index; *limit = w.limit; }
+        *hits += w.hits;
+    }
+    cudaSetDevice(prev);
+    return st;
+}
+
+mq_status mq_check_selftest(int32_t device) {
+    if (mq_device_count() <= device || device < 0) return MQ_ERR_NO_DEVICE;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    if (cudaSetDevice(device) != cudaSuccess) { cudaGetLastError(); return MQ_ERR_CUDA; }
+    const int r = mq_check_selftest_launch();
+    cudaSetDevice(prev);
+    return r == 0 ? MQ_OK : (r == -3 ? MQ_ERR_NOMEM : MQ_ERR_CUDA);
+}
+
 mq_status mq_engine_autotune(mq_engine* e, const mq_job* jobs, size_t njobs, const double dc[4], const mq_physics* ph,
                              uint64_t sample_per_job, mq_tuning* best, double* best_rate) {
     mq_status s = check_batch(e, jobs, njobs, ph);

@@ -11,6 +11,7 @@
 // (Clock::fill, world.rs:445-465), the combined DC field (Fields::dc_field,
 // channel.rs:220-226) and the per-job summary (summarize, channel.rs:496-506).
 #include "mq_internal.h"
+#include "mq_check.h"
 
 namespace mqd {
 namespace {
@@ -96,6 +97,7 @@ __global__ void __launch_bounds__(128) k_f64_step(DevGrid g, Batch b, const JobC
                     for (int dk = 0; dk < 2; ++dk) {
                         double wz = dk ? tz : 1.0 - tz;
                         size_t q = (size_t)(ci + di) + nx * ((size_t)(cj + dj) + ny * (size_t)(ck + dk));
+                        q = MQ_CHK(q, nx * ny * (size_t)g.nz, MQ_SITE_F64_FIELD);
                         double w = wx * wy * wz;
                         float4 r = __ldg(g.rf + q), a = __ldg(g.ac + q), c = __ldg(g.dc + q);
                         er[0] += w * (double)r.x; er[1] += w * (double)r.y; er[2] += w * (double)r.z;
@@ -165,6 +167,7 @@ __global__ void __launch_bounds__(128) k_f64_step(DevGrid g, Batch b, const JobC
             if (x[2] > b.crash_z0 && x[2] < b.crash_z1) {
                 int32_t ni = mqp::node_round(x[0] / h, g.nx), nj = mqp::node_round(x[1] / h, g.ny), nk = mqp::node_round(x[2] / h, g.nz);
                 size_t q = (size_t)ni + nx * ((size_t)nj + ny * (size_t)nk);
+                q = MQ_CHK(q, nx * ny * (size_t)g.nz, MQ_SITE_F64_CRASH);
                 if (__ldg(&g.rf[q].w) > 0.5f) { status = 1; break; }
             }
             if (age >= b.max_steps) { status = 5; break; }
@@ -256,3 +259,5 @@ cudaError_t launch_summarize(DevIons io, uint32_t n, uint32_t njobs, unsigned lo
 }
 
 }  // namespace mqd
+
+MQ_CHECK_READER(mq_check_read_f64)

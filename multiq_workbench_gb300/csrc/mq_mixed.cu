@@ -18,6 +18,7 @@
 //     step * f * dt mod 1), evaluated with an FP32 quarter-turn polynomial;
 //   * Philox-4x32-10 counter RNG keyed by the ion's 64-bit key, counter = step.
 #include "mq_mixed.h"
+#include "mq_check.h"
 
 #include <cstring>
 #include <vector>
@@ -124,7 +125,8 @@ __device__ __forceinline__ void load_cell(const float4* __restrict__ nodes, cons
     uint32_t m = 0;
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
-        const size_t o = 3 * (base + (size_t)(q & 1) + ((q & 2) ? sy : 0) + ((q & 4) ? sz : 0));
+        size_t o = 3 * (base + (size_t)(q & 1) + ((q & 2) ? sy : 0) + ((q & 4) ? sz : 0));
+        o = MQ_CHK_SPAN(o, 3, 3 * sz * (size_t)B.nz, MQ_SITE_MIX_CELL);
         const float4 r = __ldg(nodes + o), d = __ldg(nodes + o + 1), a = __ldg(nodes + o + 2);
         c.R[0][q] = r.x; c.R[1][q] = r.y; c.R[2][q] = r.z;
         c.D[0][q] = d.x; c.D[1][q] = d.y; c.D[2][q] = d.z;
@@ -208,7 +210,7 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
             if (!have && !drained) {
                 const uint32_t slot = base + __popc(need & ((1u << lane) - 1u));
                 if (slot < count) {
-                    id = __ldg(list_in + slot);
+                    id = (uint32_t)MQ_CHK(__ldg(list_in + slot), n_all, MQ_SITE_MIX_ION);
                     jid = io.jid[id];
                     const MixJob J = jobs[jid];
                     kick = J.kick; v_ac = J.use_ac ? J.v_ac : 0.0f; cand_a = J.cand_a; cand_b = J.cand_b;
@@ -429,7 +431,7 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
             uint32_t base = 0;
             if ((int)lane == leader) base = atomicAdd(count_out, (uint32_t)__popc(am));
             base = __shfl_sync(FULL, base, leader);
-            if (append) list_out[base + __popc(am & ((1u << lane) - 1u))] = id;
+            if (append) list_out[MQ_CHK(base + __popc(am & ((1u << lane) - 1u)), n_all, MQ_SITE_MIX_LIST_OUT)] = id;
         }
     }
 #pragma unroll
@@ -698,3 +700,5 @@ cudaError_t run(Scratch& s, const Tuning& t, DevGrid g, uint64_t grid_gen, const
 }
 
 }  // namespace mqmix
+
+MQ_CHECK_READER(mq_check_read_mixed)

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include "mq_engine.h"
+#include "mq_check.h"
 
 namespace {
 
@@ -26,7 +27,25 @@ __global__ void __launch_bounds__(512) k_l2_read(const float4* __restrict__ buf,
     if (acc == -1.0f) atomicAdd(sink, 1u);   // the buffer holds zeros: never taken, keeps the loads
 }
 
+// one index equal to its limit, through the check (no memory is accessed): a check build records it
+__global__ void k_check_selftest(unsigned long long* out) {
+    out[0] = (unsigned long long)MQ_CHK(7u, 7u, MQ_SITE_SELFTEST);
+}
+
 }  // namespace
+
+MQ_CHECK_READER(mq_check_read_probe)
+
+extern "C" int mq_check_selftest_launch(void) {
+    unsigned long long* d = nullptr;
+    if (cudaMalloc(&d, sizeof(unsigned long long)) != cudaSuccess) { cudaGetLastError(); return -3; }
+    k_check_selftest<<<1, 1>>>(d);
+    unsigned long long h = 1;
+    const cudaError_t e = cudaMemcpy(&h, d, sizeof(h), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) { cudaGetLastError(); return -2; }
+    return 0;
+}
 
 extern "C" mq_status mq_measure_l2_read_gbs(int32_t device, size_t bytes, int32_t passes, double* gbs) {
     if (!gbs || passes < 1 || passes > 10000 || bytes < ((size_t)16 << 20) || bytes > ((size_t)96 << 20))

@@ -15,6 +15,7 @@
 #include "mq_phys.h"
 #include "mq_tandem.h"
 #include "mq_tandem_internal.h"
+#include "mq_check.h"
 
 namespace {
 
@@ -66,7 +67,8 @@ __device__ void cube_field(const TConst& C, const float4* dc, const double x[3],
     for (int k = 0; k < 2; ++k)
         for (int j = 0; j < 2; ++j)
             for (int i = 0; i < 2; ++i) {
-                const size_t q = (size_t)(c[0] + i) + (size_t)C.cn[0] * ((size_t)(c[1] + j) + (size_t)C.cn[1] * (size_t)(c[2] + k));
+                size_t q = (size_t)(c[0] + i) + (size_t)C.cn[0] * ((size_t)(c[1] + j) + (size_t)C.cn[1] * (size_t)(c[2] + k));
+                q = MQ_CHK(q, (size_t)C.cn[0] * (size_t)C.cn[1] * (size_t)C.cn[2], MQ_SITE_TDM_CUBE);
                 const double wt = (i == 1 ? w[0] : 1.0 - w[0]) * (j == 1 ? w[1] : 1.0 - w[1]) * (k == 1 ? w[2] : 1.0 - w[2]);
                 const float4 r = C.crf[q], d = dc[q];
                 e[0] += wt * (rf * (double)r.x + (double)d.x);
@@ -89,7 +91,8 @@ __device__ void chan_field(const TPort& P, double gate_v, const double x[3], dou
             const double wy = dj ? ty : 1.0 - ty;
             for (int dk = 0; dk < 2; ++dk) {
                 const double wz = dk ? tz : 1.0 - tz;
-                const size_t q = (size_t)(i0 + di) + nx * ((size_t)(j0 + dj) + ny * (size_t)(k0 + dk));
+                size_t q = (size_t)(i0 + di) + nx * ((size_t)(j0 + dj) + ny * (size_t)(k0 + dk));
+                q = MQ_CHK(q, nx * ny * (size_t)P.kn[2], MQ_SITE_TDM_PORT);
                 const double w = wx * wy * wz;
                 const float4 r = P.rf[q], a = P.ac[q], d = P.dc[q];
                 er[0] += w * (double)r.x; er[1] += w * (double)r.y; er[2] += w * (double)r.z;
@@ -103,7 +106,8 @@ __device__ void chan_field(const TPort& P, double gate_v, const double x[3], dou
         for (int ii = 0; ii < 2; ++ii)
             for (int jj = 0; jj < 2; ++jj)
                 for (int kk = 0; kk < 2; ++kk) {
-                    const size_t q = (size_t)(i0 + ii) + nx * ((size_t)(j0 + jj) + ny * (size_t)(k0 + kk));
+                    size_t q = (size_t)(i0 + ii) + nx * ((size_t)(j0 + jj) + ny * (size_t)(k0 + kk));
+                    q = MQ_CHK(q, nx * ny * (size_t)P.kn[2], MQ_SITE_TDM_GATE);
                     const double w = gate_v * (ii == 1 ? tx : 1.0 - tx) * (jj == 1 ? ty : 1.0 - ty) * (kk == 1 ? tz : 1.0 - tz);
                     const float4 b = P.gate[q];
                     bias[0] += w * (double)b.x; bias[1] += w * (double)b.y; bias[2] += w * (double)b.z;
@@ -117,7 +121,8 @@ __device__ bool chan_crash(const TPort& P, const double x[3]) {   // world.rs:30
         if (x[d] < 0.0 || x[d] > P.lim[d]) return true;
     const int32_t ni = mqp::node_round(x[0] / P.kh, P.kn[0]), nj = mqp::node_round(x[1] / P.kh, P.kn[1]),
                   nk = mqp::node_round(x[2] / P.kh, P.kn[2]);
-    const size_t q = (size_t)ni + (size_t)P.kn[0] * ((size_t)nj + (size_t)P.kn[1] * (size_t)nk);
+    size_t q = (size_t)ni + (size_t)P.kn[0] * ((size_t)nj + (size_t)P.kn[1] * (size_t)nk);
+    q = MQ_CHK(q, (size_t)P.kn[0] * (size_t)P.kn[1] * (size_t)P.kn[2], MQ_SITE_TDM_CRASH);
     return P.rf[q].w > 0.5f;
 }
 
@@ -521,3 +526,5 @@ mq_status mq_tandem_advance(mq_tandem* t, mq_tracks* tr, size_t n, uint64_t step
 }
 
 }  // extern "C"
+
+MQ_CHECK_READER(mq_check_read_tandem)

@@ -23,6 +23,7 @@
 #include "mq_cube_geom.h"
 #include "mq_phys.h"
 #include "mq_tandem_internal.h"
+#include "mq_check.h"
 
 namespace mqtm {
 namespace {
@@ -227,7 +228,8 @@ __device__ __forceinline__ void cell_for(const RegK& k, int reg, const float xh[
         if (k.cube) {
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
-                const size_t o = 2 * (base + (size_t)(q & 1) + ((q & 2) ? sy : 0) + ((q & 4) ? sz : 0));
+                size_t o = 2 * (base + (size_t)(q & 1) + ((q & 2) ? sy : 0) + ((q & 4) ? sz : 0));
+                o = MQ_CHK_SPAN(o, 2, 2 * sz * (size_t)k.nz, MQ_SITE_TMX_CELL);
                 const float4 r = __ldg(k.rec + o), d = __ldg(k.rec + o + 1);
                 c.R[0][q] = r.x; c.R[1][q] = r.y; c.R[2][q] = r.z;
                 c.D[0][q] = d.x; c.D[1][q] = d.y; c.D[2][q] = d.z;
@@ -235,7 +237,8 @@ __device__ __forceinline__ void cell_for(const RegK& k, int reg, const float xh[
         } else {
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
-                const size_t o = 3 * (base + (size_t)(q & 1) + ((q & 2) ? sy : 0) + ((q & 4) ? sz : 0));
+                size_t o = 3 * (base + (size_t)(q & 1) + ((q & 2) ? sy : 0) + ((q & 4) ? sz : 0));
+                o = MQ_CHK_SPAN(o, 3, 3 * sz * (size_t)k.nz, MQ_SITE_TMX_CELL);
                 const float4 r = __ldg(k.rec + o), d = __ldg(k.rec + o + 1), a = __ldg(k.rec + o + 2);
                 c.R[0][q] = r.x; c.R[1][q] = r.y; c.R[2][q] = r.z;
                 c.D[0][q] = d.x; c.D[1][q] = d.y; c.D[2][q] = d.z;
@@ -319,7 +322,7 @@ __global__ void k_tm_bucket(const int32_t* __restrict__ region, uint32_t n, uint
     uint32_t base = 0;
     if ((int)lane == leader) base = atomicAdd(&bcount[r], (uint32_t)__popc(peers));
     base = __shfl_sync(peers, base, leader);
-    list[(size_t)r * n + base + __popc(peers & ((1u << lane) - 1u))] = i;
+    list[MQ_CHK((size_t)r * n + base + __popc(peers & ((1u << lane) - 1u)), (size_t)kBuckets * n, MQ_SITE_TMX_LIST)] = i;
 }
 
 // one chunk of global steps for every live track (one thread per track, grouped by region)
@@ -339,7 +342,7 @@ __global__ void __launch_bounds__(128, 3) k_tm_step(TMConst C, MTracks M, uint32
     if (t < off[kBuckets]) {
         int r0 = 0;
         while (r0 < kBuckets - 1 && t >= off[r0 + 1]) ++r0;
-        const uint32_t id = list[(size_t)r0 * n + (t - off[r0])];
+        const uint32_t id = (uint32_t)MQ_CHK(list[(size_t)r0 * n + (t - off[r0])], n, MQ_SITE_TMX_LIST);
         int reg = r0, last = M.last[id];
         const int sp = M.sp[id];
         const uint64_t key = M.key[id];
@@ -776,3 +779,5 @@ cudaError_t run(State* s, uint32_t n, const float* drive, uint64_t step0, uint64
 }
 
 }  // namespace mqtm
+
+MQ_CHECK_READER(mq_check_read_tandem_mixed)
