@@ -421,7 +421,7 @@ mq_status mq_engine_create(const mq_grid_desc* g, int32_t precision, int32_t dev
     }
     if (cudaMalloc((void**)&e->d_dc, bytes) != cudaSuccess) { cudaGetLastError(); return bail(MQ_ERR_NOMEM); }
     if (cudaMemset(e->d_dc, 0, bytes) != cudaSuccess) return bail(MQ_ERR_CUDA);
-    e->tune = mqmix::default_tuning(device);
+    e->tune = mqmix::default_tuning(device, e->nnodes);
     *out = e;
     return MQ_OK;
 }
@@ -677,7 +677,7 @@ mq_status mq_engine_autotune(mq_engine* e, const mq_job* jobs, size_t njobs, con
     const mqmix::Tuning keep = e->tune;
     mqmix::Tuning top = keep;
     double top_rate = -1.0;
-    const int blocks[] = {2, 3};
+    const int blocks[] = {1, 2, 3};
     const uint32_t chunks[] = {2048, 8192, 20000};
     for (int pf = 0; pf < 2; ++pf)
     for (int bl : blocks)

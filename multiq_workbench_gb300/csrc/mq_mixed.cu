@@ -550,11 +550,18 @@ MixBatch make_mix_batch(const mqp::Batch& b) {
     return m;
 }
 
-Tuning default_tuning(int device) {
+Tuning default_tuning(int device, size_t nodes) {
     Tuning t;
     int sms = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) { cudaGetLastError(); sms = 1; }
     t.sms = sms;
+    // Resident ions per SM by the size of the node records: on grids far larger than L2 the
+    // gathers of fewer ions in flight hit the caches more often than more warps hide latency
+    // (measured on the channel at 0.100 / 0.050 / 0.0333 mm, 0.30 / 2.4 / 8.0 GB of records:
+    // best at 3 / 2 / 1 blocks per SM, 28.7 / 17.9 / 9.8 G ion-steps/s against 28.7 / 11.1 / 6.4
+    // with 3 everywhere).
+    const double rec = 48.0 * (double)nodes;
+    t.blocks_per_sm = rec < 1.0e9 ? 3 : (rec < 4.0e9 ? 2 : 1);
     return t;
 }
 

@@ -39,7 +39,7 @@ struct MixBatch {      // per-batch constants (device-resident parameter block)
 
 struct Tuning {
     int tpb = 128;             // threads per block
-    int blocks_per_sm = 3;     // resident blocks per SM for the persistent grid (168 registers/thread)
+    int blocks_per_sm = 3;     // resident blocks per SM for the persistent grid (168 registers/thread; 3 at most)
     uint32_t chunk = 20000;    // steps per ion per launch (compaction interval)
     int use_graph = 1;         // replay the launch sequence as one CUDA graph
     int prefetch = 0;          // L1-prefetch the cell an ion is heading for
@@ -76,7 +76,7 @@ struct RunInfo {
 
 MixJob make_mix_job(const mqp::JobC& j, const mqp::Batch& b);
 MixBatch make_mix_batch(const mqp::Batch& b);
-Tuning default_tuning(int device);
+Tuning default_tuning(int device, size_t nodes);
 cudaError_t run(Scratch& s, const Tuning& t, mqd::DevGrid g, uint64_t grid_gen, const mqp::Batch& b, const MixJob* jobs,
                 size_t njobs, mqd::DevIons io, uint32_t n, uint32_t max_more, cudaStream_t st, RunInfo* info);
 void release(Scratch& s);
