@@ -623,6 +623,11 @@ cudaError_t run(Scratch& s, const Tuning& t, DevGrid g, uint64_t grid_gen, const
     *info = RunInfo();
     if (n == 0) return cudaSuccess;
     if (t.tpb != 128) return cudaErrorInvalidValue;   // the kernel is compiled for 128-thread blocks
+    // the kernel uses no shared memory: ask for the largest L1 (the cell gathers of neighbouring
+    // ions hit there; measured +4.7% / +4.4% on the 0.100 / 0.050 mm grids over the default split)
+    for (const void* fn : {(const void*)k_mixed<false, false>, (const void*)k_mixed<true, false>,
+                           (const void*)k_mixed<false, true>, (const void*)k_mixed<true, true>})
+        if ((e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 0)) != cudaSuccess) return e;
     if ((e = pack_nodes(s, g, grid_gen, st, &info->kernel_launches)) != cudaSuccess) return e;
     const size_t list_bytes = (size_t)2 * n * sizeof(uint32_t);
     if (s.list_cap < list_bytes) {

@@ -767,6 +767,9 @@ cudaError_t run(State* s, uint32_t n, const float* drive, uint64_t step0, uint64
     cudaError_t e;
     if (!n) return cudaSuccess;
     const unsigned grid = (n + 127) / 128;
+    // the step kernel needs a few words of shared memory: ask for the largest L1 for the gathers
+    if ((e = cudaFuncSetAttribute((const void*)k_tm_step, cudaFuncAttributePreferredSharedMemoryCarveout, 0)) != cudaSuccess)
+        return e;
     for (uint64_t q = 0; q < k; q += kChunk) {
         const uint32_t S = (uint32_t)(k - q < kChunk ? k - q : kChunk);
         if ((e = cudaMemsetAsync(s->bcount, 0, kBuckets * sizeof(uint32_t), st)) != cudaSuccess) return e;
