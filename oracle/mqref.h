@@ -1,7 +1,8 @@
 /*
  * mqref -- CPU oracle for the batched ion-trajectory path.  TEST INFRASTRUCTURE ONLY:
  * used by tests/, __graft_entry__.smoke() and bench.py's cpu_baseline / reference arm
- * as the checker and the timed host baseline.  The product never links or calls it.
+ * as the reference results of the parity tests and the timed host baseline.  The product
+ * never links or calls it.
  *
  * A plain-C FP64 restatement of the reference integrator of filiprumenovski/multiq-workbench:
  *   simulation/mqviz/src/world.rs:265-288   World::fields_at (one pass over 8 corners)

@@ -1,8 +1,8 @@
 """ctypes binding of the CPU oracle (``oracle/mqref.c``).  TEST INFRASTRUCTURE ONLY: used
-by tests/, ``__graft_entry__.smoke()`` and bench.py's CPU baseline as the checker.
+by tests/, ``__graft_entry__.smoke()`` and bench.py's CPU baseline for the reference results.
 
 The oracle takes the same inputs as the engine (a solved grid, jobs, physics, SoA ion
-states) in its own C structs, so a checker never routes through product code.
+states) in its own C structs, so a parity test never routes through product code.
 """
 from __future__ import annotations
 

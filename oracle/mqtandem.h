@@ -1,6 +1,7 @@
 /*
  * mqtandem -- CPU oracle for the nine-channel tandem transport.  TEST INFRASTRUCTURE ONLY:
- * used by tests/ and bench.py's CPU baseline as the checker; the product never links it.
+ * used by tests/ and bench.py's CPU baseline for the reference results; the product never
+ * links it.
  *
  * A plain-C FP64 restatement of trapsim (filiprumenovski/multiq-workbench):
  *   simulation/trapsim/src/geometry.rs:12-16     electrode ids

@@ -1,8 +1,8 @@
 """ctypes binding of the tandem oracle (``oracle/mqtandem.c``).  TEST INFRASTRUCTURE ONLY:
-used by tests/ and bench.py's CPU baseline as the checker of the tandem transport.
+used by tests/ and bench.py's CPU baseline for the reference results of the tandem transport.
 
 The oracle's C structs have the same memory layout as the engine's ``mq_tandem_desc`` and
-``mq_tracks``; a checker copies the bytes of a description into the oracle's own struct, so
+``mq_tracks``; a test copies the bytes of a description into the oracle's own struct, so
 no oracle call routes through product code.
 """
 from __future__ import annotations

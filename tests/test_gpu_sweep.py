@@ -10,7 +10,7 @@ pytestmark = pytest.mark.gpu
 
 
 class OracleEngine:
-    """run_batch over the CPU oracle (the checker)."""
+    """run_batch over the CPU oracle."""
 
     def __init__(self, f):
         self.f = f
