@@ -343,7 +343,7 @@ mq_status run_f64(mq_engine* e, const Batch& b, uint32_t tlen, size_t n, uint32_
 }
 
 mq_status run_mixed(mq_engine* e, const mq_job* jobs, size_t njobs, const mq_physics& ph, const Batch& b, size_t n,
-                    uint32_t max_more, mq_run_stats* stats, uint64_t* steps_out) {
+                    uint32_t max_more, int write_states, mq_run_stats* stats, uint64_t* steps_out) {
     std::vector<mqmix::MixJob> mj(njobs);
     for (size_t k = 0; k < njobs; ++k) mj[k] = mqmix::make_mix_job(make_job(jobs[k], ph), b);
     const int32_t fault = e->fault;
@@ -357,7 +357,7 @@ mq_status run_mixed(mq_engine* e, const mq_job* jobs, size_t njobs, const mq_phy
     }
     mqmix::RunInfo info;
     cudaError_t c = mqmix::run(e->mix, tune, dev_grid(e), e->grid_gen, b, mj.data(), njobs, dev_ions(e), (uint32_t)n,
-                               max_more, e->st, &info);
+                               max_more, write_states, e->st, &info);
     if (c != cudaSuccess) return cuda_fail(e, c, "mixed engine");
     *steps_out = info.ion_steps;
     if (info.watchdog)
@@ -512,7 +512,7 @@ mq_status mq_run_ions(mq_engine* e, const mq_job* jobs, size_t njobs, const mq_p
     if ((s = upload_jobs(e, jobs, njobs, *ph, b, false, &tlen, &ntab, &h2d)) != MQ_OK) return s;
     uint64_t steps = 0;
     if (e->prec == MQ_PREC_F64) s = run_f64(e, b, tlen, n, max_more, stats, &steps);
-    else s = run_mixed(e, jobs, njobs, *ph, b, n, max_more, stats, &steps);
+    else s = run_mixed(e, jobs, njobs, *ph, b, n, max_more, 1, stats, &steps);
     if (s == MQ_ERR_WATCHDOG) {   // the states are the checkpoint: hand them back so the caller can resume
         const std::string why = e->err;
         mq_status s2 = copy_ions(e, io, n, false, &d2h);
@@ -560,7 +560,7 @@ mq_status mq_run_batch(mq_engine* e, const mq_job* jobs, size_t njobs, const dou
     CK(mqd::launch_inject(b, jt, dev_ions(e), (uint32_t)n, e->st), "inject kernel");
     uint64_t steps = 0;
     if (e->prec == MQ_PREC_F64) s = run_f64(e, b, tlen, n, 0xFFFFFFFFu, stats, &steps);
-    else s = run_mixed(e, jobs, njobs, *ph, b, n, 0xFFFFFFFFu, stats, &steps);
+    else s = run_mixed(e, jobs, njobs, *ph, b, n, 0xFFFFFFFFu, ions_out ? 1 : 0, stats, &steps);
     if (s != MQ_OK) return s;
     CK(e->counters.grow(sizeof(unsigned long long) * mqd::kCounters * njobs), "job counters");
     CK(cudaMemsetAsync(e->counters.p, 0, sizeof(unsigned long long) * mqd::kCounters * njobs, e->st), "counter reset");

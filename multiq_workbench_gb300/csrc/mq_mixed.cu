@@ -168,9 +168,11 @@ template <bool LEGACY, bool PREFETCH>
 __global__ void __launch_bounds__(128, 3)
 k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__ jobs, DevIons io,
         const uint32_t* __restrict__ list_in, uint32_t* __restrict__ list_out, Ctrs* ctr, int in_slot, uint32_t chunk,
-        float* __restrict__ keep, uint32_t n_all, int resume) {
-    // keep: exact double-float position/velocity of ions re-queued by an earlier launch of the
-    // same call (12 floats per ion, structure of arrays over n_all); resume != 0 reads it
+        float* __restrict__ keep, const uint64_t* __restrict__ kph, uint32_t n_all) {
+    // keep: the working state of every ion of the call in grid units, double-float position and
+    // velocity (12 floats per ion, structure of arrays over n_all), filled from the FP64 states by
+    // k_init_list and written back to them by k_unstage, so this kernel does no FP64 arithmetic;
+    // kph: the RF / AC phase offsets as 64-bit fixed-point turns (two arrays of n_all)
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t count = ctr->count[in_slot];
     if (count == 0) return;
@@ -217,24 +219,13 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
                     Wac = ((uint64_t)J.w_ac_hi << 32) | J.w_ac_lo;
                     cw_ac = J.cw_ac; sw_ac = J.sw_ac;
                     n = io.steps[id]; ncoll = io.ncoll[id]; leg = io.leg[id];
-                    if (resume) {
 #pragma unroll
-                        for (int d = 0; d < 3; ++d) {
-                            xh[d] = keep[(size_t)(0 + d) * n_all + id]; xl[d] = keep[(size_t)(3 + d) * n_all + id];
-                            uh[d] = keep[(size_t)(6 + d) * n_all + id]; ul[d] = keep[(size_t)(9 + d) * n_all + id];
-                        }
-                    } else {
-                        const double gx[3] = {io.x[id] * B.inv_h, io.y[id] * B.inv_h, io.z[id] * B.inv_h};
-                        const double gu[3] = {io.vx[id] * B.v2u, io.vy[id] * B.v2u, io.vz[id] * B.v2u};
-#pragma unroll
-                        for (int d = 0; d < 3; ++d) {
-                            xh[d] = (float)gx[d]; xl[d] = (float)(gx[d] - (double)xh[d]);
-                            uh[d] = (float)gu[d]; ul[d] = (float)(gu[d] - (double)uh[d]);
-                        }
+                    for (int d = 0; d < 3; ++d) {
+                        xh[d] = keep[(size_t)(0 + d) * n_all + id]; xl[d] = keep[(size_t)(3 + d) * n_all + id];
+                        uh[d] = keep[(size_t)(6 + d) * n_all + id]; ul[d] = keep[(size_t)(9 + d) * n_all + id];
                     }
                     // phase = offset + n * w (mod 1) in 64-bit fixed point
-                    const double prf = io.ph_rf[id], pac = io.ph_ac[id];
-                    const uint64_t orf = (uint64_t)(prf * 0x1.0p63) << 1, oac = (uint64_t)(pac * 0x1.0p63) << 1;
+                    const uint64_t orf = kph[id], oac = kph[(size_t)n_all + id];
                     Prf = orf + (uint64_t)n * Wrf;
                     Pac = oac + (uint64_t)n * Wac;
                     // drive state as an uninterrupted run has it: exact at the last step that is
@@ -404,23 +395,16 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
                 if (status == 0 && n >= B.max_steps) status = 5;
             }
             if (status != 0 || done >= chunk) {
-                // ---- write back (FP64 state, same layout as the FP64 engine)
-                io.x[id] = ((double)xh[0] + (double)xl[0]) * B.h;
-                io.y[id] = ((double)xh[1] + (double)xl[1]) * B.h;
-                io.z[id] = ((double)xh[2] + (double)xl[2]) * B.h;
-                io.vx[id] = ((double)uh[0] + (double)ul[0]) * B.u2v;
-                io.vy[id] = ((double)uh[1] + (double)ul[1]) * B.u2v;
-                io.vz[id] = ((double)uh[2] + (double)ul[2]) * B.u2v;
+                // ---- write back: counters to the ion states, position and velocity to the working
+                //      state (k_unstage turns it into the FP64 state when the caller wants that)
                 io.steps[id] = n; io.ncoll[id] = ncoll; io.leg[id] = leg; io.status[id] = status;
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    keep[(size_t)(0 + d) * n_all + id] = xh[d]; keep[(size_t)(3 + d) * n_all + id] = xl[d];
+                    keep[(size_t)(6 + d) * n_all + id] = uh[d]; keep[(size_t)(9 + d) * n_all + id] = ul[d];
+                }
                 steps_total += done;
                 append = status == 0;
-                if (append && keep) {
-#pragma unroll
-                    for (int d = 0; d < 3; ++d) {
-                        keep[(size_t)(0 + d) * n_all + id] = xh[d]; keep[(size_t)(3 + d) * n_all + id] = xl[d];
-                        keep[(size_t)(6 + d) * n_all + id] = uh[d]; keep[(size_t)(9 + d) * n_all + id] = ul[d];
-                    }
-                }
                 have = false;
             }
         }
@@ -459,10 +443,26 @@ __global__ void k_pack_nodes(const float4* __restrict__ rf, const float4* __rest
     nodes[3 * q + 2] = ac[q];
 }
 
-// initial live list: ions with status 0, warp-ballot compaction
-__global__ void k_init_list(DevIons io, uint32_t n, uint32_t* list, Ctrs* ctr) {
+// initial live list (ions with status 0, warp-ballot compaction) and their working state: the
+// FP64 position / velocity in grid units as double-floats and the phase offsets as fixed-point
+// turns, converted here with every lane of a warp busy instead of one lane at a time in k_mixed
+__global__ void k_init_list(DevIons io, uint32_t n, uint32_t* list, Ctrs* ctr, MixBatch B, float* __restrict__ keep,
+                            uint64_t* __restrict__ kph, uint8_t* __restrict__ staged) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool live = i < n && io.status[i] == 0;
+    if (i < n) staged[i] = live ? 1 : 0;
+    if (live) {
+        const double gx[3] = {io.x[i] * B.inv_h, io.y[i] * B.inv_h, io.z[i] * B.inv_h};
+        const double gu[3] = {io.vx[i] * B.v2u, io.vy[i] * B.v2u, io.vz[i] * B.v2u};
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const float xh = (float)gx[d], uh = (float)gu[d];
+            keep[(size_t)(0 + d) * n + i] = xh; keep[(size_t)(3 + d) * n + i] = (float)(gx[d] - (double)xh);
+            keep[(size_t)(6 + d) * n + i] = uh; keep[(size_t)(9 + d) * n + i] = (float)(gu[d] - (double)uh);
+        }
+        kph[i] = (uint64_t)(io.ph_rf[i] * 0x1.0p63) << 1;
+        kph[(size_t)n + i] = (uint64_t)(io.ph_ac[i] * 0x1.0p63) << 1;
+    }
     const unsigned m = __ballot_sync(FULL, live);
     const uint32_t lane = threadIdx.x & 31;
     if (m) {
@@ -471,6 +471,20 @@ __global__ void k_init_list(DevIons io, uint32_t n, uint32_t* list, Ctrs* ctr) {
         if ((int)lane == leader) base = atomicAdd(&ctr->count[0], (uint32_t)__popc(m));
         base = __shfl_sync(FULL, base, leader);
         if (live) list[base + __popc(m & ((1u << lane) - 1u))] = i;
+    }
+}
+
+// FP64 position and velocity of every ion staged at the start of the call, from its working state
+__global__ void k_unstage(DevIons io, uint32_t n, MixBatch B, const float* __restrict__ keep,
+                          const uint8_t* __restrict__ staged) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || !staged[i]) return;
+    double* const xs[3] = {io.x, io.y, io.z};
+    double* const vs[3] = {io.vx, io.vy, io.vz};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        xs[d][i] = ((double)keep[(size_t)(0 + d) * n + i] + (double)keep[(size_t)(3 + d) * n + i]) * B.h;
+        vs[d][i] = ((double)keep[(size_t)(6 + d) * n + i] + (double)keep[(size_t)(9 + d) * n + i]) * B.u2v;
     }
 }
 
@@ -579,7 +593,8 @@ static cudaError_t enqueue_launches(const Scratch& s, const Tuning& t, const Mix
     Ctrs* ctr = static_cast<Ctrs*>(s.ctrs);
     const MixJob* jobs = static_cast<const MixJob*>(s.jobs);
     const float4* nodes = static_cast<const float4*>(s.nodes);
-    float* keep = static_cast<float*>(s.keep);
+    uint64_t* kph = static_cast<uint64_t*>(s.keep);
+    float* keep = reinterpret_cast<float*>(kph + (size_t)2 * n);
     const int grid = t.sms * t.blocks_per_sm;
     for (uint32_t L = 0; L < launches; ++L) {
         const int in = (int)(L & 1);
@@ -588,11 +603,11 @@ static cudaError_t enqueue_launches(const Scratch& s, const Tuning& t, const Mix
         const uint32_t* li = lists + (size_t)in * n;
         uint32_t* lo = lists + (size_t)(in ^ 1) * n;
         if (mb.legacy_coll) {
-            if (t.prefetch) k_mixed<true, true><<<grid, t.tpb, 0, st>>>(nodes, mb, jobs, io, li, lo, ctr, in, ch, keep, n, L > 0);
-            else k_mixed<true, false><<<grid, t.tpb, 0, st>>>(nodes, mb, jobs, io, li, lo, ctr, in, ch, keep, n, L > 0);
+            if (t.prefetch) k_mixed<true, true><<<grid, t.tpb, 0, st>>>(nodes, mb, jobs, io, li, lo, ctr, in, ch, keep, kph, n);
+            else k_mixed<true, false><<<grid, t.tpb, 0, st>>>(nodes, mb, jobs, io, li, lo, ctr, in, ch, keep, kph, n);
         } else {
-            if (t.prefetch) k_mixed<false, true><<<grid, t.tpb, 0, st>>>(nodes, mb, jobs, io, li, lo, ctr, in, ch, keep, n, L > 0);
-            else k_mixed<false, false><<<grid, t.tpb, 0, st>>>(nodes, mb, jobs, io, li, lo, ctr, in, ch, keep, n, L > 0);
+            if (t.prefetch) k_mixed<false, true><<<grid, t.tpb, 0, st>>>(nodes, mb, jobs, io, li, lo, ctr, in, ch, keep, kph, n);
+            else k_mixed<false, false><<<grid, t.tpb, 0, st>>>(nodes, mb, jobs, io, li, lo, ctr, in, ch, keep, kph, n);
         }
         *kernels += 2;
     }
@@ -618,7 +633,7 @@ cudaError_t pack_nodes(Scratch& s, DevGrid g, uint64_t grid_gen, cudaStream_t st
 }
 
 cudaError_t run(Scratch& s, const Tuning& t, DevGrid g, uint64_t grid_gen, const mqp::Batch& b, const MixJob* jobs,
-                size_t njobs, DevIons io, uint32_t n, uint32_t max_more, cudaStream_t st, RunInfo* info) {
+                size_t njobs, DevIons io, uint32_t n, uint32_t max_more, int write_states, cudaStream_t st, RunInfo* info) {
     cudaError_t e;
     *info = RunInfo();
     if (n == 0) return cudaSuccess;
@@ -653,8 +668,9 @@ cudaError_t run(Scratch& s, const Tuning& t, DevGrid g, uint64_t grid_gen, const
     const uint32_t full = (uint32_t)((need + chunk - 1) / chunk);
     const uint32_t launches = (t.max_launches && t.max_launches < full) ? t.max_launches : full;
     const uint32_t last_chunk = launches < full ? chunk : (uint32_t)(need - (uint64_t)(launches - 1) * chunk);
-    // exact double-float state of re-queued ions (only when the call spans several launches)
-    const size_t keep_bytes = launches > 1 ? (size_t)12 * n * sizeof(float) : 0;
+    // working state: phase offsets (2 x u64), position / velocity double-floats (12 x f32) and the
+    // staged flag (u8) of every ion
+    const size_t keep_bytes = (size_t)n * (2 * sizeof(uint64_t) + 12 * sizeof(float) + 1);
     if (s.keep_cap < keep_bytes) {
         if (s.keep) cudaFree(s.keep);
         s.keep = nullptr; s.keep_cap = 0;
@@ -663,7 +679,10 @@ cudaError_t run(Scratch& s, const Tuning& t, DevGrid g, uint64_t grid_gen, const
     }
     Ctrs* ctr = static_cast<Ctrs*>(s.ctrs);
     if ((e = cudaMemsetAsync(ctr, 0, sizeof(Ctrs), st)) != cudaSuccess) return e;
-    k_init_list<<<(n + 255) / 256, 256, 0, st>>>(io, n, static_cast<uint32_t*>(s.lists), ctr);
+    uint64_t* kph = static_cast<uint64_t*>(s.keep);
+    float* keep = reinterpret_cast<float*>(kph + (size_t)2 * n);
+    uint8_t* staged = reinterpret_cast<uint8_t*>(keep + (size_t)12 * n);
+    k_init_list<<<(n + 255) / 256, 256, 0, st>>>(io, n, static_cast<uint32_t*>(s.lists), ctr, mb, keep, kph, staged);
     info->kernel_launches += 1;
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     cudaEventRecord(s.ev[0], st);
@@ -697,6 +716,11 @@ cudaError_t run(Scratch& s, const Tuning& t, DevGrid g, uint64_t grid_gen, const
         if ((e = enqueue_launches(s, t, mb, io, n, launches, chunk, last_chunk, st, &kernels)) != cudaSuccess) return e;
     }
     cudaEventRecord(s.ev[1], st);
+    if (write_states) {
+        k_unstage<<<(n + 255) / 256, 256, 0, st>>>(io, n, mb, keep, staged);
+        info->kernel_launches += 1;
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
     Ctrs h;
     if ((e = cudaMemcpyAsync(&h, ctr, sizeof(Ctrs), cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;

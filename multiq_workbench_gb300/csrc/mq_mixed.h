@@ -54,7 +54,7 @@ struct Scratch {
     void* params = nullptr;    // MixBatch
     void* jobs = nullptr;      // MixJob[]
     size_t jobs_cap = 0;
-    void* keep = nullptr;      // exact double-float state of ions re-queued between launches
+    void* keep = nullptr;      // working state of the call's ions (phase offsets, double-floats, staged flags)
     size_t keep_cap = 0;
     void* nodes = nullptr;     // interleaved RF | DC | AC node records (float4 x 3 per node)
     size_t nodes_cap = 0;
@@ -77,8 +77,11 @@ struct RunInfo {
 MixJob make_mix_job(const mqp::JobC& j, const mqp::Batch& b);
 MixBatch make_mix_batch(const mqp::Batch& b);
 Tuning default_tuning(int device, size_t nodes);
+// write_states = 0 leaves the FP64 position / velocity of the ion states as they were (a caller
+// that wants only the counters, steps, status and collision counts)
 cudaError_t run(Scratch& s, const Tuning& t, mqd::DevGrid g, uint64_t grid_gen, const mqp::Batch& b, const MixJob* jobs,
-                size_t njobs, mqd::DevIons io, uint32_t n, uint32_t max_more, cudaStream_t st, RunInfo* info);
+                size_t njobs, mqd::DevIons io, uint32_t n, uint32_t max_more, int write_states, cudaStream_t st,
+                RunInfo* info);
 void release(Scratch& s);
 
 }  // namespace mqmix
