@@ -131,6 +131,38 @@ def test_mixed_deterministic(coarse):
     _assert_bitequal(a, b, "mixed run twice")
 
 
+def test_ragged_and_empty_jobs(coarse):
+    """Jobs of 1, 0, 33, 2, 255 and 64 ions in one batch: the FP64 kernel's states equal the
+    oracle's bit for bit, both engines count every job's ions once (the empty job included), and
+    a batch whose jobs are all empty returns zero counts."""
+    mq = _mq()
+    ph = _variants()["half_kick_gauss"]
+    dc = [0.0, 5.0, -5.0, 0.0]
+    sizes = (1, 0, 33, 2, 255, 64)
+    jobs = [mq.Job(mq.Species(mz, 1.0, 2.95 * mz ** (2 / 3)), mq.RfAc(100.0, 500e3, 0.5, 99e3 + 500.0 * k), nn, 500 + k)
+            for k, (mz, nn) in enumerate(zip((491.0, 493.0, 497.0, 499.0, 503.0, 507.0), sizes))]
+    ref = _oracle_run(coarse, jobs, ph, dc)
+    with mq.Engine(coarse, mq.PREC_F64) as e:
+        ions, _ = e.run_batch_ions(jobs, dc, ph)
+        _assert_bitequal(ions, ref, "ragged FP64 vs oracle")
+        out = e.run_batch(jobs, dc, ph)
+        assert list(out.n) == list(sizes)
+        empty = e.run_batch([mq.Job(j.sp, j.drive, 0, j.seed) for j in jobs], dc, ph)
+        assert all(o.n == 0 and o.transmitted == 0 for o in empty)
+    with mq.Engine(coarse, mq.PREC_MIXED) as e:
+        out = e.run_batch(jobs, dc, ph)
+        assert list(out.n) == list(sizes)
+        assert all(o.crashed + o.returned + o.transmitted + o.left + o.timeout == o.n for o in out)
+        empty = e.run_batch([mq.Job(j.sp, j.drive, 0, j.seed) for j in jobs], dc, ph)
+        assert all(o.n == 0 for o in empty)
+        # more than 2^32 - 16 ions in one batch is refused before anything is allocated
+        huge = [mq.Job(jobs[0].sp, jobs[0].drive, 1 << 31, 1), mq.Job(jobs[0].sp, jobs[0].drive, 1 << 31, 2)]
+        with pytest.raises(mq.MqError) as ei:
+            e.run_batch(huge, dc, ph)
+        assert ei.value.code == -8
+        assert list(e.run_batch(jobs, dc, ph).n) == list(sizes)     # still usable
+
+
 def test_mixed_collision_free_tracks_fp64(coarse):
     """No gas: the mixed engine's compensated FP32 state follows the FP64 trajectory.
     Tolerance: after 300 steps |dx| <= 1e-3 cell and |dv|/|v| <= 1e-4 for ions alive in both."""
