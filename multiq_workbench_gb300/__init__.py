@@ -4,7 +4,8 @@ filiprumenovski/multiq-workbench).  Public API mirrors chsim: ``Geom``, ``Fields
 router mirrors trapsim: ``TandemModel``, ``CubeGeometry``, ``CubeFields``; ``scan`` holds chsim's
 result cache and adaptive scan, ``check`` its batch self-check; ``sweep`` runs excitation-frequency
 sweeps of a species mixture as one batch and ``fit`` turns their counts into R = f0 / FWHM (mqviz
-``fit_sweep``)."""
+``fit_sweep``); ``multiq_workbench_gb300.validate`` compares the engines at the S14 calibrated
+point with chsim's own counts (mqviz ``--validate``; also ``python -m`` runnable)."""
 from .grid import Geom, Fields, cache_dir, cache_path
 from .channel import (Engine, Species, RfAc, Job, JobTable, Physics, Outcome, Outcomes, IonStates, RunStats, MqError, summarize, inject,
                       device_count, PREC_F64, PREC_MIXED, LAUNCH_DISC, LAUNCH_LEGACY, LAUNCH_GAUSSIAN, STATUS,

@@ -2,9 +2,9 @@
 chsim's GPU counts for 100,000 ions, seed 4242, Physics::correct(0.1), t_max 3 ms, the calibrated S14
 channel and drive): the FP64 kernel reproduces the oracle's committed counts exactly (it is
 bit-exact with the oracle on the same grid, and the grid solved on the GPU is bit-identical to the
-host's), which puts it within the reference's own bar against chsim's counts (|pull| <= 2 on every
-row, validate.rs:119-135); the mixed engine, an independent random stream, agrees with both within
-3 sigma per row."""
+host's); both engines meet the reference's own bar against chsim's counts (|pull| <= 2 on its rows
+T, C, R and T/(T+C), validate.rs:119-135), and the mixed engine, an independent random stream,
+agrees with the FP64 kernel within 3 sigma on every count."""
 import json
 import math
 from pathlib import Path
@@ -21,27 +21,28 @@ def _pull(k1, n1, k2, n2):
     return (p1 - p2) / max(math.sqrt(p1 * (1 - p1) / n1 + p2 * (1 - p2) / n2), 1e-12)
 
 
-def _rows(o):
-    return {"transmitted": int(o.transmitted.sum()), "crashed_or_left": int(o.crashed.sum() + o.left.sum()),
-            "returned": int(o.returned.sum()), "timeout": int(o.timeout.sum())}
+def _as_rows(c):
+    return {"transmitted": c.trans, "crashed_or_left": c.crash, "returned": c.ret, "timeout": c.timeout}
 
 
 def test_s14_point_on_the_device(built):
     import multiq_workbench_gb300 as mq
+    from multiq_workbench_gb300 import validate as V
     s = PINS["s14_chsim_gpu"]
-    f = mq.Fields.build(mq.Geom.s14("code", hole_d=7.0), cache=False, device=0)
-    ph = mq.Physics.correct(0.1)
-    ph.t_max = 3e-3
-    jobs = [mq.Job(mq.Species(2 * 863.473, 2.0, 425.0), mq.RfAc(70.0, 500e3, 0.35, 84.25e3), s["n"], 4242)]
-    dc = [18.0, 24.0, 15.0, 20.0]
+    assert V.REF_CHSIM_GPU == (s["n"], s["transmitted"], s["crashed_or_left"], s["returned"], s["timeout"])
+    f = V.s14_fields(device=0)
     with mq.Engine(f, mq.PREC_F64) as e:
-        r64 = _rows(e.run_batch(jobs, dc, ph))
-    assert r64 == {k: s["oracle"][k] for k in r64}, (r64, s["oracle"])
+        c64 = V.run_engine(e, s["n"], 4242, rf_phase0=True)
+    assert _as_rows(c64) == {k: s["oracle"][k] for k in _as_rows(c64)}, (c64, s["oracle"])
     with mq.Engine(f, mq.PREC_MIXED) as e:
-        rm = _rows(e.run_batch(jobs, dc, ph))
+        cm = V.run_engine(e, s["n"], 4242, rf_phase0=True)
+    metal = V.embedded_metal()
+    # the reference's own rows and bar: T, C, R and T/(T+C), |pull| <= 2 (validate.rs:119-135)
+    for c in (c64, cm):
+        for row in V.rows(c, metal):
+            assert abs(row.pull()) <= 2.0, (row.name, row.live, row.refv, row.pull())
+    # the mixed engine (an independent random stream) against the FP64 kernel, timeouts included
+    for row in V.rows(cm, c64):
+        assert abs(row.pull()) <= 3.0, (row.name, row.pull())
     n = s["n"]
-    print("mixed", rm, {k: round(_pull(rm[k], n, s[k], n), 2) for k in rm})
-    for k in rm:
-        # an independent random stream: a 3-sigma bar per row against chsim's and the FP64 counts
-        assert abs(_pull(rm[k], n, s[k], n)) <= 3.0, (k, rm[k], s[k])
-        assert abs(_pull(rm[k], n, r64[k], n)) <= 3.0, (k, rm[k], r64[k])
+    assert abs(_pull(cm.timeout, n, c64.timeout, n)) <= 3.0
