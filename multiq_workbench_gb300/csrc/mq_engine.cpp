@@ -408,6 +408,11 @@ mq_status mq_engine_create(const mq_grid_desc* g, int32_t precision, int32_t dev
     for (int i = 0; i < 8; ++i) e->layers[i] = g->layers_mm[i];
     e->nnodes = (size_t)g->nx * g->ny * g->nz;
     auto bail = [&](mq_status s) { mq_engine_destroy(e); return s; };
+    // the mixed kernel addresses its 3 node records per node with 32-bit offsets
+    if (precision == MQ_PREC_MIXED && 3 * e->nnodes >= ((size_t)1 << 32)) {
+        e->err = "grid too large for the mixed engine (3 x nodes must be below 2^32)";
+        return bail(MQ_ERR_TOO_LARGE);
+    }
     if (cudaSetDevice(device) != cudaSuccess) return bail(MQ_ERR_CUDA);
     if (cudaStreamCreateWithFlags(&e->st, cudaStreamNonBlocking) != cudaSuccess) return bail(MQ_ERR_CUDA);
     for (auto& v : e->ev) if (cudaEventCreate(&v) != cudaSuccess) return bail(MQ_ERR_CUDA);

@@ -114,19 +114,21 @@ struct Cell {
     uint32_t mask;                      // conductor bit per corner
 };
 
-__device__ __forceinline__ size_t node_of(const MixBatch& B, int32_t ci, int32_t cj, int32_t ck) {
-    return (size_t)ci + (size_t)B.nx * ((size_t)cj + (size_t)B.ny * (size_t)ck);
+// record offsets are 32-bit (the host refuses grids with 3 x nodes >= 2^32): less address arithmetic
+// in the divergent reload path (measured about 1% on the sweep)
+__device__ __forceinline__ uint32_t node_of(const MixBatch& B, int32_t ci, int32_t cj, int32_t ck) {
+    return (uint32_t)ci + (uint32_t)B.nx * ((uint32_t)cj + (uint32_t)B.ny * (uint32_t)ck);
 }
 
 __device__ __forceinline__ void load_cell(const float4* __restrict__ nodes, const MixBatch& B, int32_t ci, int32_t cj,
                                           int32_t ck, Cell& c) {
-    const size_t sy = (size_t)B.nx, sz = (size_t)B.nx * (size_t)B.ny;
-    const size_t base = node_of(B, ci, cj, ck);
+    const uint32_t sy = (uint32_t)B.nx, sz = (uint32_t)B.nx * (uint32_t)B.ny;
+    const uint32_t base = node_of(B, ci, cj, ck);
     uint32_t m = 0;
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
-        size_t o = 3 * (base + (size_t)(q & 1) + ((q & 2) ? sy : 0) + ((q & 4) ? sz : 0));
-        o = MQ_CHK_SPAN(o, 3, 3 * sz * (size_t)B.nz, MQ_SITE_MIX_CELL);
+        uint32_t o = 3u * (base + (uint32_t)(q & 1) + ((q & 2) ? sy : 0u) + ((q & 4) ? sz : 0u));
+        o = (uint32_t)MQ_CHK_SPAN(o, 3, 3 * (size_t)sz * (size_t)B.nz, MQ_SITE_MIX_CELL);
         const float4 r = __ldg(nodes + o), d = __ldg(nodes + o + 1), a = __ldg(nodes + o + 2);
         c.R[0][q] = r.x; c.R[1][q] = r.y; c.R[2][q] = r.z;
         c.D[0][q] = d.x; c.D[1][q] = d.y; c.D[2][q] = d.z;
@@ -139,8 +141,8 @@ __device__ __forceinline__ void load_cell(const float4* __restrict__ nodes, cons
 
 // pull the 4 corner runs of a cell into L1 ahead of use
 __device__ __forceinline__ void prefetch_cell(const float4* nodes, const MixBatch& B, int32_t ci, int32_t cj, int32_t ck) {
-    const size_t sy = (size_t)B.nx, sz = (size_t)B.nx * (size_t)B.ny;
-    const size_t base = node_of(B, ci, cj, ck);
+    const uint32_t sy = (uint32_t)B.nx, sz = (uint32_t)B.nx * (uint32_t)B.ny;
+    const uint32_t base = node_of(B, ci, cj, ck);
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
         const float4* p = nodes + 3 * (base + ((r & 1) ? sy : 0) + ((r & 2) ? sz : 0));
@@ -638,11 +640,6 @@ cudaError_t run(Scratch& s, const Tuning& t, DevGrid g, uint64_t grid_gen, const
     *info = RunInfo();
     if (n == 0) return cudaSuccess;
     if (t.tpb != 128) return cudaErrorInvalidValue;   // the kernel is compiled for 128-thread blocks
-    // the kernel uses no shared memory: ask for the largest L1 (the cell gathers of neighbouring
-    // ions hit there; measured +4.7% / +4.4% on the 0.100 / 0.050 mm grids over the default split)
-    for (const void* fn : {(const void*)k_mixed<false, false>, (const void*)k_mixed<true, false>,
-                           (const void*)k_mixed<false, true>, (const void*)k_mixed<true, true>})
-        if ((e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 0)) != cudaSuccess) return e;
     if ((e = pack_nodes(s, g, grid_gen, st, &info->kernel_launches)) != cudaSuccess) return e;
     const size_t list_bytes = (size_t)2 * n * sizeof(uint32_t);
     if (s.list_cap < list_bytes) {

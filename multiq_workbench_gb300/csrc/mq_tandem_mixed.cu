@@ -222,14 +222,15 @@ __device__ __forceinline__ void cell_for(const RegK& k, int reg, const float xh[
     const int ci = clampi(__float2int_rd(xh[0]), 0, k.nx - 2), cj = clampi(__float2int_rd(xh[1]), 0, k.ny - 2),
               ck = clampi(__float2int_rd(xh[2]), 0, k.nz - 2);
     if (ci != c.ci || cj != c.cj || ck != c.ck || reg != c.reg) {
-        const size_t sy = (size_t)k.nx, sz = (size_t)k.nx * (size_t)k.ny;
-        const size_t base = (size_t)ci + sy * (size_t)cj + sz * (size_t)ck;
+        // 32-bit record offsets (the host refuses grids with 3 x nodes >= 2^32)
+        const uint32_t sy = (uint32_t)k.nx, sz = (uint32_t)k.nx * (uint32_t)k.ny;
+        const uint32_t base = (uint32_t)ci + sy * (uint32_t)cj + sz * (uint32_t)ck;
         uint32_t m = 0;
         if (k.cube) {
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
-                size_t o = 2 * (base + (size_t)(q & 1) + ((q & 2) ? sy : 0) + ((q & 4) ? sz : 0));
-                o = MQ_CHK_SPAN(o, 2, 2 * sz * (size_t)k.nz, MQ_SITE_TMX_CELL);
+                uint32_t o = 2u * (base + (uint32_t)(q & 1) + ((q & 2) ? sy : 0u) + ((q & 4) ? sz : 0u));
+                o = (uint32_t)MQ_CHK_SPAN(o, 2, 2 * (size_t)sz * (size_t)k.nz, MQ_SITE_TMX_CELL);
                 const float4 r = __ldg(k.rec + o), d = __ldg(k.rec + o + 1);
                 c.R[0][q] = r.x; c.R[1][q] = r.y; c.R[2][q] = r.z;
                 c.D[0][q] = d.x; c.D[1][q] = d.y; c.D[2][q] = d.z;
@@ -237,8 +238,8 @@ __device__ __forceinline__ void cell_for(const RegK& k, int reg, const float xh[
         } else {
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
-                size_t o = 3 * (base + (size_t)(q & 1) + ((q & 2) ? sy : 0) + ((q & 4) ? sz : 0));
-                o = MQ_CHK_SPAN(o, 3, 3 * sz * (size_t)k.nz, MQ_SITE_TMX_CELL);
+                uint32_t o = 3u * (base + (uint32_t)(q & 1) + ((q & 2) ? sy : 0u) + ((q & 4) ? sz : 0u));
+                o = (uint32_t)MQ_CHK_SPAN(o, 3, 3 * (size_t)sz * (size_t)k.nz, MQ_SITE_TMX_CELL);
                 const float4 r = __ldg(k.rec + o), d = __ldg(k.rec + o + 1), a = __ldg(k.rec + o + 2);
                 c.R[0][q] = r.x; c.R[1][q] = r.y; c.R[2][q] = r.z;
                 c.D[0][q] = d.x; c.D[1][q] = d.y; c.D[2][q] = d.z;
@@ -633,6 +634,7 @@ State* create(const mq_tandem_desc& d, const DevFields& f, cudaStream_t st, std:
     G.ext_axis = g.ext_axis; G.ext_side = g.ext_side; G.ext_cell0 = g.ext_cell[0]; G.ext_cell1 = g.ext_cell[1];
     // cube grid and the two region DC sets
     const size_t cn = (size_t)d.cube_dims[0] * d.cube_dims[1] * d.cube_dims[2];
+    if (3 * cn >= ((size_t)1 << 32)) return fail("cube grid too large for 32-bit record offsets", cudaErrorInvalidValue);
     for (int a = 0; a < 3; ++a) {
         C.cn[a] = d.cube_dims[a];
         C.clo[a] = (float)d.cube_lo_mm[a];
@@ -692,6 +694,7 @@ State* create(const mq_tandem_desc& d, const DevFields& f, cudaStream_t st, std:
             if (m.rf == k.rf && m.ac == k.ac && m.dc == k.dc && m.gate == k.gate && m.idle == k.idle) P.rec = m.rec;
         if (!P.rec) {
             const size_t nodes = (size_t)P.nx * P.ny * P.nz;
+            if (3 * nodes >= ((size_t)1 << 32)) return fail("port grid too large for 32-bit record offsets", cudaErrorInvalidValue);
             void* p = nullptr;
             if ((e = cudaMalloc(&p, nodes * 48)) != cudaSuccess) return fail("port records", e);
             s->allocs.push_back(p);
@@ -767,9 +770,6 @@ cudaError_t run(State* s, uint32_t n, const float* drive, uint64_t step0, uint64
     cudaError_t e;
     if (!n) return cudaSuccess;
     const unsigned grid = (n + 127) / 128;
-    // the step kernel needs a few words of shared memory: ask for the largest L1 for the gathers
-    if ((e = cudaFuncSetAttribute((const void*)k_tm_step, cudaFuncAttributePreferredSharedMemoryCarveout, 0)) != cudaSuccess)
-        return e;
     for (uint64_t q = 0; q < k; q += kChunk) {
         const uint32_t S = (uint32_t)(k - q < kChunk ? k - q : kChunk);
         if ((e = cudaMemsetAsync(s->bcount, 0, kBuckets * sizeof(uint32_t), st)) != cudaSuccess) return e;

@@ -69,8 +69,9 @@ def test_alloc_and_launch_failures_are_status_codes(coarse, prec):
 
 
 def test_grid_larger_than_the_device_is_refused(built):
-    """Engine creation on a 4096^3 grid (1.1 TB per field) fails at the first device allocation,
-    before any host array is read, and returns MQ_ERR_NOMEM."""
+    """Engine creation on a 4096^3 grid (1.1 TB per field): the FP64 engine fails at the first device
+    allocation, before any host array is read, with MQ_ERR_NOMEM; the mixed engine refuses it before
+    that with MQ_ERR_TOO_LARGE (its record offsets are 32-bit)."""
     import ctypes as C
     from multiq_workbench_gb300 import _native as N
     small = np.zeros(16, np.float32)
@@ -79,5 +80,7 @@ def test_grid_larger_than_the_device_is_refused(built):
     g.h = 1e-4
     g.rf4 = g.ac4 = small.ctypes.data
     h = C.c_void_p()
-    assert N.lib().mq_engine_create(C.byref(g), 1, 0, C.byref(h)) == -3
+    assert N.lib().mq_engine_create(C.byref(g), 0, 0, C.byref(h)) == -3
+    assert not h.value
+    assert N.lib().mq_engine_create(C.byref(g), 1, 0, C.byref(h)) == -8
     assert not h.value
