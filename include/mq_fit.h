@@ -23,6 +23,7 @@
  *                                                                        simulation/mqviz/src/world.rs:187-231
  *   mq_terrain_compute        <- terrain::compute                        simulation/mqviz/src/terrain.rs:40-55
  *   mq_terrain_dfdmz          <- analysis::dfdmz                         simulation/mqviz/src/analysis.rs:10-18
+ *   mq_secular_freq           <- chsim secular_freq                      simulation/chsim/src/channel.rs:555-578
  */
 #ifndef MQ_FIT_H
 #define MQ_FIT_H
@@ -110,6 +111,15 @@ int32_t mq_terrain_compute(size_t n, size_t cap, const double* rf2, const double
  * difference of m -> m (1 +- 1 %). */
 double mq_terrain_dfdmz(size_t n, size_t cap, const double* z_mm, const double* rf2, const double* dc2, double mass,
                         double charge, double v_rf, const double dc[4], double f_rf);
+
+/* Secular frequency [Hz] from a trajectory (chsim secular_freq, simulation/chsim/src/channel.rs:555-578):
+ * an FP64 ion of charge-to-mass qm [C/kg] released at rest 0.2 mm off the axis (x = y = axis_m) along
+ * (1, -1)/sqrt2 in the z = z_m slice of the RF field (rf4: float4 E per volt, grid spacing h [m]),
+ * driven by v_rf sin(2 pi f_rf t) with the transverse force only, 200 steps per RF period for 4 ms;
+ * the frequency of the upward zero crossings of x - y.  *out = NaN when the ion leaves the 2.5 mm
+ * window or crosses fewer than three times.  Indices are clamped to the grid. */
+int32_t mq_secular_freq(const float* rf4, int32_t nx, int32_t ny, int32_t nz, double h, double axis_m, double qm,
+                        double v_rf, double f_rf, double z_m, double* out);
 
 #ifdef __cplusplus
 }

@@ -244,6 +244,8 @@ def _declare_fit(L) -> None:
     L.mq_terrain_compute.restype = i32
     L.mq_terrain_dfdmz.argtypes = [sz, sz, vp, vp, vp, d, d, d, vp, d]
     L.mq_terrain_dfdmz.restype = d
+    L.mq_secular_freq.argtypes = [vp, i32, i32, i32, d, d, d, d, d, d, P(d)]
+    L.mq_secular_freq.restype = i32
 
 
 def _declare_tandem(L) -> None:

@@ -581,4 +581,50 @@ double mq_terrain_dfdmz(size_t n, size_t cap, const double* z_mm, const double* 
     return (fx[k] - fx[n + k]) / (2.0 * eps * (mass / charge));
 }
 
+int32_t mq_secular_freq(const float* rf4, int32_t nx, int32_t ny, int32_t nz, double h, double axis_m, double qm,
+                        double v_rf, double f_rf, double z_m, double* out) {
+    if (!rf4 || !out || nx < 2 || ny < 2 || nz < 2 || !(h > 0.0) || !(f_rf > 0.0)) return MQ_ERR_INVALID;
+    auto tri = [&](const double x[3], double e[3]) {
+        const double g[3] = {x[0] / h, x[1] / h, x[2] / h};
+        auto cell = [](double gg, int n) {
+            const double c = gg > 0.0 ? std::floor(gg) : 0.0;
+            return c >= (double)(n - 2) ? (size_t)(n - 2) : (size_t)c;
+        };
+        const size_t i = cell(g[0], nx), j = cell(g[1], ny), k = cell(g[2], nz);
+        const double tx = g[0] - (double)i, ty = g[1] - (double)j, tz = g[2] - (double)k;
+        e[0] = e[1] = e[2] = 0.0;
+        for (int di = 0; di < 2; ++di)
+            for (int dj = 0; dj < 2; ++dj)
+                for (int dk = 0; dk < 2; ++dk) {
+                    const double wx = di ? tx : 1.0 - tx, wy = dj ? ty : 1.0 - ty, wz = dk ? tz : 1.0 - tz;
+                    const size_t q = (i + di) + (size_t)nx * ((j + dj) + (size_t)ny * (k + dk));
+                    for (int d = 0; d < 3; ++d) e[d] += wx * wy * wz * (double)rf4[4 * q + d];
+                }
+    };
+    const double a = axis_m, amp = 0.2e-3, w = kTau * f_rf;
+    double x[3] = {a + amp / std::sqrt(2.0), a - amp / std::sqrt(2.0), z_m};
+    double v[3] = {0.0, 0.0, 0.0};
+    const double dt = 1.0 / f_rf / 200.0;
+    const size_t n = (size_t)(4e-3 / dt);
+    std::vector<double> cross;
+    double prev = (x[0] - a) - (x[1] - a);
+    double t = 0.0;
+    *out = NAN;
+    for (size_t s = 0; s < n; ++s) {
+        double e[3];
+        tri(x, e);
+        const double sn = v_rf * std::sin(w * t);
+        for (int d = 0; d < 2; ++d) v[d] += qm * sn * e[d] * dt;   // transverse only: z frozen at the slice
+        for (int d = 0; d < 2; ++d) x[d] += v[d] * dt;
+        t += dt;
+        const double u = (x[0] - a) - (x[1] - a);
+        if (prev < 0.0 && u >= 0.0) cross.push_back(t);
+        prev = u;
+        if (std::fabs(x[0] - a) > 2.5e-3 || std::fabs(x[1] - a) > 2.5e-3) return MQ_OK;
+    }
+    if (cross.size() < 3) return MQ_OK;
+    *out = (double)(cross.size() - 1) / (cross.back() - cross.front());
+    return MQ_OK;
+}
+
 }  // extern "C"

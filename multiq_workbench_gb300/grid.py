@@ -161,10 +161,15 @@ class SolveInfo:
 class Fields:
     """Per-volt basis fields of a geometry (chsim ``Fields``): float32 arrays of shape (n, 4)."""
 
-    def __init__(self, geom: Geom, nx: int, ny: int, nz: int, h: float, rf, ac, dc, info=None):
+    def __init__(self, geom: Geom, nx: int, ny: int, nz: int, h: float, rf, ac, dc, info=None, axis_phi=None,
+                 rf_phi_near=None):
         self.geom, self.nx, self.ny, self.nz, self.h = geom, nx, ny, nz, h
         self.rf, self.ac, self.dc = rf, ac, list(dc)
         self.info: list[SolveInfo] = info or []
+        # potentials kept from the solve: each basis on the axis column (i = j = nx / 2), and the RF
+        # basis in a (2w + 1)^2 window around it (w >= 5 nodes and >= 0.5 mm) for the r0 fits
+        self.axis_phi: dict = axis_phi or {}
+        self.rf_phi_near = rf_phi_near
 
     @property
     def n(self) -> int:
@@ -184,6 +189,7 @@ class Fields:
         out = {}
         info = []
         mask = None
+        axis_phi, near = {}, None
         for b in want:
             e4 = np.zeros((n, 4), np.float32)
             phi = np.empty(n, np.float64)
@@ -213,8 +219,27 @@ class Fields:
                     except OSError:
                         pass
             out[b] = e4
+            p3 = phi.reshape(nz, ny, nx)
+            a = nx // 2
+            axis_phi[b] = p3[:, a, a].copy()
+            if b == 0:
+                w = near_window(geom.h_mm)
+                near = p3[:, max(a - w, 0):a + w + 1, max(a - w, 0):a + w + 1].copy()
         dc = [out.get(b) for b in (2, 3, 4, 5)]
-        return cls(geom, nx, ny, nz, geom.h_mm * 1e-3, out[0], out[1], dc, info)
+        return cls(geom, nx, ny, nz, geom.h_mm * 1e-3, out[0], out[1], dc, info, axis_phi, near)
+
+    def dc_phi_axis(self, v) -> list:
+        """On-axis static potential for DC voltages [q1, plate, down, box]: (z_mm, phi) per node
+        (channel.rs:227-230)."""
+        out = []
+        for k in range(self.nz):
+            p = 0.0
+            for b in range(4):
+                col = self.axis_phi.get(2 + b)
+                if col is not None:
+                    p += float(v[b]) * float(col[k])
+            out.append((k * self.geom.h_mm, p))
+        return out
 
     def dc_field(self, v) -> np.ndarray:
         """Combined static DC field for voltages [q1, plate, down, box] (channel.rs:219-226)."""
@@ -235,6 +260,11 @@ class Fields:
         for k in range(8):
             d.layers_mm[k] = lay[k]
         return d
+
+
+def near_window(h_mm: float) -> int:
+    """Half-width in nodes of the RF window kept around the axis: at least 5 nodes and 0.5 mm."""
+    return max(5, int(round(0.5 / h_mm)))
 
 
 def replace(g: Geom, **kw) -> Geom:
