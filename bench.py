@@ -421,10 +421,12 @@ def run_tandem(args, rank: int, world: int):
     m, wl = tandem_setup(args, rank, mq.PREC_MIXED)
     m.device = local
     pulse = m.tracks.copy()
+    work = m.tracks.copy(pinned=True)   # the advance's host buffers: page-locked, filled from the pulse
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
 
     def one(model=m):
-        model.tracks = pulse.copy()
+        work.copy_from(pulse)
+        model.tracks = work
         model.step = 0
         model.counts = type(model.counts)()
         t0 = time.perf_counter()

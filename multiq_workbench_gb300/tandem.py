@@ -226,10 +226,18 @@ class Tracks:
     """Structure-of-arrays track states (region 0 split, 1..9 port, 10 combine, 11 lost, 12 back,
     13 detected; ``last`` = port of the last rejection or -1)."""
 
-    def __init__(self, n: int):
+    def __init__(self, n: int, pinned: bool = False):
         self.n = int(n)
+        self.pinned = bool(pinned)
+        self._keep = []
         for k, dt in TRACK_FIELDS:
-            setattr(self, k, np.zeros(self.n, dt))
+            if pinned:
+                import torch   # page-locked host memory for the host<->device copies of an advance
+                t = torch.zeros(self.n * np.dtype(dt).itemsize, dtype=torch.uint8, pin_memory=True)
+                self._keep.append(t)
+                setattr(self, k, np.frombuffer(t.numpy(), dtype=dt, count=self.n))
+            else:
+                setattr(self, k, np.zeros(self.n, dt))
 
     def __len__(self) -> int:
         return self.n
@@ -240,11 +248,17 @@ class Tracks:
             setattr(t, k, getattr(self, k).ctypes.data)
         return t
 
-    def copy(self) -> "Tracks":
-        t = Tracks(self.n)
-        for k, _ in TRACK_FIELDS:
-            setattr(t, k, getattr(self, k).copy())
+    def copy(self, pinned: bool | None = None) -> "Tracks":
+        t = Tracks(self.n, self.pinned if pinned is None else pinned)
+        t.copy_from(self)
         return t
+
+    def copy_from(self, other: "Tracks") -> None:
+        """Overwrite these states with another set of the same size, in place."""
+        if other.n != self.n:
+            raise ValueError("track counts differ")
+        for k, _ in TRACK_FIELDS:
+            np.copyto(getattr(self, k), getattr(other, k))
 
 
 @dataclass
