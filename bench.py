@@ -136,7 +136,7 @@ def run_gridstudy(args, rank: int, world: int):
             agree = float(np.mean(ions_m.status == ions_d.status))
         nodes = f.nx * f.ny * f.nz
         grids.append({"h_mm": h, "dims": [f.nx, f.ny, f.nz], "nodes": nodes,
-                      "node_records_gb": nodes * 48 / 1e9, "solve_s": t_solve,
+                      "node_records_gb": nodes * (64 if tuned["wide_records"] else 48) / 1e9, "solve_s": t_solve,
                       "tuning": tuned,
                       "mixed": {"value": rate, "unit": UNIT, "ms_per_step": float(np.mean(ms)),
                                 "e2e": steps / float(np.mean(walls)), "ion_steps": int(steps),

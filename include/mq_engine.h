@@ -126,6 +126,8 @@ typedef struct mq_tuning {
     uint32_t chunk;              /* steps per ion per launch (compaction interval)         */
     int32_t use_graph;           /* replay the launch sequence as one CUDA graph           */
     int32_t prefetch;            /* L1-prefetch the cell each ion is heading for           */
+    int32_t wide_records;        /* 64-byte node records read with 256-bit loads (else 48 B;
+                                    needs 4 x nodes below 2^32)                            */
 } mq_tuning;
 mq_status   mq_engine_get_tuning(mq_engine* e, mq_tuning* t);
 mq_status   mq_engine_set_tuning(mq_engine* e, const mq_tuning* t);

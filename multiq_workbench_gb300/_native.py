@@ -106,7 +106,8 @@ class mq_dev_grid(C.Structure):
 
 class mq_tuning(C.Structure):
     _fields_ = [("threads_per_block", C.c_int32), ("blocks_per_sm", C.c_int32), ("chunk", C.c_uint32),
-                ("use_graph", C.c_int32), ("prefetch", C.c_int32)]
+                ("use_graph", C.c_int32), ("prefetch", C.c_int32),
+                ("wide_records", C.c_int32)]
 
 
 class mq_cube_geom(C.Structure):

@@ -408,7 +408,7 @@ mq_status mq_engine_create(const mq_grid_desc* g, int32_t precision, int32_t dev
     for (int i = 0; i < 8; ++i) e->layers[i] = g->layers_mm[i];
     e->nnodes = (size_t)g->nx * g->ny * g->nz;
     auto bail = [&](mq_status s) { mq_engine_destroy(e); return s; };
-    // the mixed kernel addresses its 3 node records per node with 32-bit offsets
+    // the mixed kernel addresses its 3 (or 4, wide) float4 of node record per node with 32-bit offsets
     if (precision == MQ_PREC_MIXED && 3 * e->nnodes >= ((size_t)1 << 32)) {
         e->err = "grid too large for the mixed engine (3 x nodes must be below 2^32)";
         return bail(MQ_ERR_TOO_LARGE);
@@ -603,6 +603,7 @@ mq_status mq_engine_get_tuning(mq_engine* e, mq_tuning* t) {
     t->chunk = e->tune.chunk;
     t->use_graph = e->tune.use_graph;
     t->prefetch = e->tune.prefetch;
+    t->wide_records = e->tune.wide;
     return MQ_OK;
 }
 
@@ -610,11 +611,14 @@ mq_status mq_engine_set_tuning(mq_engine* e, const mq_tuning* t) {
     if (!e || !t) return MQ_ERR_INVALID;
     if (t->threads_per_block != 128 || t->blocks_per_sm < 1 || t->blocks_per_sm > 3 || t->chunk == 0)
         return fail(e, MQ_ERR_INVALID, "tuning: 128 threads per block, 1..3 blocks per SM, chunk > 0");
+    if (t->wide_records && 4 * e->nnodes >= ((size_t)1 << 32))
+        return fail(e, MQ_ERR_INVALID, "tuning: wide node records need 4 x nodes below 2^32");
     e->tune.tpb = t->threads_per_block;
     e->tune.blocks_per_sm = t->blocks_per_sm;
     e->tune.chunk = t->chunk;
     e->tune.use_graph = t->use_graph ? 1 : 0;
     e->tune.prefetch = t->prefetch ? 1 : 0;
+    e->tune.wide = t->wide_records ? 1 : 0;
     return MQ_OK;
 }
 
@@ -684,6 +688,8 @@ mq_status mq_engine_autotune(mq_engine* e, const mq_job* jobs, size_t njobs, con
     double top_rate = -1.0;
     const int blocks[] = {1, 2, 3};
     const uint32_t chunks[] = {2048, 8192, 20000};
+    const int widths = 4 * e->nnodes < ((size_t)1 << 32) ? 2 : 1;
+    for (int wd = 0; wd < widths; ++wd)
     for (int pf = 0; pf < 2; ++pf)
     for (int bl : blocks)
         for (uint32_t ch : chunks) {
@@ -691,6 +697,7 @@ mq_status mq_engine_autotune(mq_engine* e, const mq_job* jobs, size_t njobs, con
             e->tune.blocks_per_sm = bl;
             e->tune.chunk = ch;
             e->tune.prefetch = pf;
+            e->tune.wide = wd;
             mq_run_stats st;
             // first call warms the graph and caches; the second is timed
             if ((s = mq_run_batch(e, sj.data(), njobs, dc, ph, out.data(), nullptr, &st)) != MQ_OK) { e->tune = keep; return s; }

@@ -10,7 +10,7 @@
 //   * positions in grid units and velocities in cells per step, each an FP32 double-float
 //     (compensated two-sum accumulator); field nodes, interpolation and collision
 //     kinematics in FP32;
-//   * fields as 48-byte interleaved node records; the 8 corners of the ion's cell x
+//   * fields as 64-byte interleaved node records; the 8 corners of the ion's cell x
 //     {RF, DC, AC} held in registers and reloaded only when the ion changes cell (the
 //     cached conductor bits of the corners give the nearest-node crash test), with an L1
 //     prefetch of the cell the ion is heading for;
@@ -104,9 +104,13 @@ __device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& 
 }
 
 // ---------------------------------------------------------------- cell cache
-// Interleaved node records: node q occupies float4 [3q] = {RF.xyz, conductor mask},
-// [3q+1] = {combined DC.xyz, conductor bits of the cell based at q}, [3q+2] = {AC.xyz, 0}
-// (48 B), so the 8 corners of a cell are 4 runs of 96 contiguous bytes.
+// Interleaved node records: node q occupies float4 [Sq] = {RF.xyz, conductor mask},
+// [Sq+1] = {combined DC.xyz, conductor bits of the cell based at q}, [Sq+2] = {AC.xyz, 0}, with
+// a record stride S of 3 float4 (48 B) or 4 (64 B, the last float4 spare), so the 8 corners of a
+// cell are 4 runs of 2 records. Wide records are 64-byte aligned and read with two 256-bit loads
+// each (16 loads a reload instead of 24): faster where the cell reloads hit L2 (about 5% on the
+// 0.100 mm channel), slower on fine grids whose gathers reach HBM and pay for the 33% larger
+// footprint (0.050 mm: 10.7 against 17.3 G ion-steps/s).
 struct Cell {
     float R[3][8], D[3][8], A[3][8];   // corner values per field and component, corner q = a + 2b + 4c
     int32_t ci, cj, ck;
@@ -114,22 +118,37 @@ struct Cell {
     uint32_t mask;                      // conductor bit per corner
 };
 
-// record offsets are 32-bit (the host refuses grids with 3 x nodes >= 2^32): less address arithmetic
+// record offsets are 32-bit (the host refuses grids with S x nodes >= 2^32): less address arithmetic
 // in the divergent reload path (measured about 1% on the sweep)
 __device__ __forceinline__ uint32_t node_of(const MixBatch& B, int32_t ci, int32_t cj, int32_t ck) {
     return (uint32_t)ci + (uint32_t)B.nx * ((uint32_t)cj + (uint32_t)B.ny * (uint32_t)ck);
 }
 
+// 32 bytes from a 32-byte aligned address (ld.global.nc.v8.f32, sm_100 and later): two float4
+__device__ __forceinline__ void ld256(const float4* p, float4& a, float4& b) {
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w) : "l"(p));
+}
+
+template <bool WIDE>
 __device__ __forceinline__ void load_cell(const float4* __restrict__ nodes, const MixBatch& B, int32_t ci, int32_t cj,
                                           int32_t ck, Cell& c) {
+    constexpr uint32_t S = WIDE ? 4u : 3u;
     const uint32_t sy = (uint32_t)B.nx, sz = (uint32_t)B.nx * (uint32_t)B.ny;
     const uint32_t base = node_of(B, ci, cj, ck);
     uint32_t m = 0;
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
-        uint32_t o = 3u * (base + (uint32_t)(q & 1) + ((q & 2) ? sy : 0u) + ((q & 4) ? sz : 0u));
-        o = (uint32_t)MQ_CHK_SPAN(o, 3, 3 * (size_t)sz * (size_t)B.nz, MQ_SITE_MIX_CELL);
-        const float4 r = __ldg(nodes + o), d = __ldg(nodes + o + 1), a = __ldg(nodes + o + 2);
+        uint32_t o = S * (base + (uint32_t)(q & 1) + ((q & 2) ? sy : 0u) + ((q & 4) ? sz : 0u));
+        o = (uint32_t)MQ_CHK_SPAN(o, S, S * (size_t)sz * (size_t)B.nz, MQ_SITE_MIX_CELL);
+        float4 r, d, a;
+        if (WIDE) {
+            float4 spare;
+            ld256(nodes + o, r, d);        // 64-byte records: both loads are 32-byte aligned
+            ld256(nodes + o + 2, a, spare);
+        } else {
+            r = __ldg(nodes + o); d = __ldg(nodes + o + 1); a = __ldg(nodes + o + 2);
+        }
         c.R[0][q] = r.x; c.R[1][q] = r.y; c.R[2][q] = r.z;
         c.D[0][q] = d.x; c.D[1][q] = d.y; c.D[2][q] = d.z;
         c.A[0][q] = a.x; c.A[1][q] = a.y; c.A[2][q] = a.z;
@@ -140,14 +159,15 @@ __device__ __forceinline__ void load_cell(const float4* __restrict__ nodes, cons
 }
 
 // pull the 4 corner runs of a cell into L1 ahead of use
+template <bool WIDE>
 __device__ __forceinline__ void prefetch_cell(const float4* nodes, const MixBatch& B, int32_t ci, int32_t cj, int32_t ck) {
     const uint32_t sy = (uint32_t)B.nx, sz = (uint32_t)B.nx * (uint32_t)B.ny;
     const uint32_t base = node_of(B, ci, cj, ck);
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
-        const float4* p = nodes + 3 * (base + ((r & 1) ? sy : 0) + ((r & 2) ? sz : 0));
+        const float4* p = nodes + (WIDE ? 4 : 3) * (base + ((r & 1) ? sy : 0) + ((r & 2) ? sz : 0));
         asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
-        asm volatile("prefetch.global.L1 [%0];" ::"l"(p + 5));
+        asm volatile("prefetch.global.L1 [%0];" ::"l"(p + (WIDE ? 7 : 5)));
     }
 }
 
@@ -166,7 +186,7 @@ __device__ __forceinline__ float field_comp(const float R[8], const float D[8], 
 __device__ __forceinline__ int32_t clampi(int32_t v, int32_t lo, int32_t hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
 // ---------------------------------------------------------------- the persistent worker
-template <bool LEGACY, bool PREFETCH>
+template <bool LEGACY, bool PREFETCH, bool WIDE>
 __global__ void __launch_bounds__(128, 3)
 k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__ jobs, DevIons io,
         const uint32_t* __restrict__ list_in, uint32_t* __restrict__ list_out, Ctrs* ctr, int in_slot, uint32_t chunk,
@@ -241,7 +261,7 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
                     const uint64_t key = io.rng[id];
                     k0 = (uint32_t)key; k1 = (uint32_t)(key >> 32);
                     if (!LEGACY) { rc = philox(k0, k1, n >> 2, 0u, 0u, 0u); rn = philox(k0, k1, (n >> 2) + 1u, 0u, 0u, 0u); }
-                    load_cell(nodes, B, clampi(__float2int_rd(xh[0]), 0, B.nx - 2), clampi(__float2int_rd(xh[1]), 0, B.ny - 2),
+                    load_cell<WIDE>(nodes, B, clampi(__float2int_rd(xh[0]), 0, B.nx - 2), clampi(__float2int_rd(xh[1]), 0, B.ny - 2),
                               clampi(__float2int_rd(xh[2]), 0, B.nz - 2), c);
                     done = 0;
                     have = true;
@@ -369,13 +389,13 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
             if (ffi != c.fci || ffj != c.fcj || ffk != c.fck) {
                 const int32_t ci = clampi(__float2int_rd(xh[0]), 0, B.nx - 2), cj = clampi(__float2int_rd(xh[1]), 0, B.ny - 2),
                               ck = clampi(__float2int_rd(xh[2]), 0, B.nz - 2);
-                if (ci != c.ci || cj != c.cj || ck != c.ck) load_cell(nodes, B, ci, cj, ck, c);
+                if (ci != c.ci || cj != c.cj || ck != c.ck) load_cell<WIDE>(nodes, B, ci, cj, ck, c);
             }
             if (PREFETCH) {
                 const int32_t pi = clampi(__float2int_rd(xh[0] + uh[0]), 0, B.nx - 2);
                 const int32_t pj = clampi(__float2int_rd(xh[1] + uh[1]), 0, B.ny - 2);
                 const int32_t pk = clampi(__float2int_rd(xh[2] + uh[2]), 0, B.nz - 2);
-                if (pi != c.ci || pj != c.cj || pk != c.ck) prefetch_cell(nodes, B, pi, pj, pk);
+                if (pi != c.ci || pj != c.cj || pk != c.ck) prefetch_cell<WIDE>(nodes, B, pi, pj, pk);
             }
             // ---- termination tests: exit, return, box, conductor, timeout
             // (a position exactly on a threshold is resolved by the high part alone; the box
@@ -425,14 +445,16 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
     if (lane == 0 && steps_total) atomicAdd(&ctr->steps, steps_total);
 }
 
-// interleave RF | combined DC | AC into 48-byte node records (once per DC configuration); the
-// spare w of the DC record holds the conductor bits of the 8 corners of the cell whose lowest
-// corner is this node (bit a + 2b + 4c), so a cell reload reads its crash mask in one word
+// interleave RF | combined DC | AC into node records of `stride` float4 (once per DC configuration
+// and record width); the spare w of the DC record holds the conductor bits of the 8 corners of the
+// cell whose lowest corner is this node (bit a + 2b + 4c), so a cell reload reads its crash mask in
+// one word
 __global__ void k_pack_nodes(const float4* __restrict__ rf, const float4* __restrict__ dc, const float4* __restrict__ ac,
-                             float4* __restrict__ nodes, size_t n, int32_t nx, int32_t ny, int32_t nz) {
+                             float4* __restrict__ nodes, size_t n, int32_t nx, int32_t ny, int32_t nz, int stride) {
     const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= n) return;
-    nodes[3 * q] = rf[q];
+    nodes[stride * q] = rf[q];
+    if (stride == 4) nodes[4 * q + 3] = make_float4(0.f, 0.f, 0.f, 0.f);
     float4 d = dc[q];
     const size_t sy = (size_t)nx, sz = (size_t)nx * (size_t)ny;
     const int32_t i = (int32_t)(q % sy), j = (int32_t)((q / sy) % (size_t)ny), k = (int32_t)(q / sz);
@@ -441,8 +463,8 @@ __global__ void k_pack_nodes(const float4* __restrict__ rf, const float4* __rest
         for (int c = 0; c < 8; ++c)
             m |= (rf[q + (size_t)(c & 1) + ((c & 2) ? sy : 0) + ((c & 4) ? sz : 0)].w > 0.5f ? 1u : 0u) << c;
     d.w = __uint_as_float(m);
-    nodes[3 * q + 1] = d;
-    nodes[3 * q + 2] = ac[q];
+    nodes[stride * q + 1] = d;
+    nodes[stride * q + 2] = ac[q];
 }
 
 // initial live list (ions with status 0, warp-ballot compaction) and their working state: the
@@ -573,11 +595,13 @@ Tuning default_tuning(int device, size_t nodes) {
     t.sms = sms;
     // Resident ions per SM by the size of the node records: on grids far larger than L2 the
     // gathers of fewer ions in flight hit the caches more often than more warps hide latency
-    // (measured on the channel at 0.100 / 0.050 / 0.0333 mm, 0.30 / 2.4 / 8.0 GB of records:
-    // best at 3 / 2 / 1 blocks per SM, 28.7 / 17.9 / 9.8 G ion-steps/s against 28.7 / 11.1 / 6.4
-    // with 3 everywhere).
+    // (measured on the channel at 0.100 / 0.050 / 0.0333 mm, 0.30 / 2.4 / 8.0 GB of 48-byte
+    // records: best at 3 / 2 / 1 blocks per SM, 28.7 / 17.9 / 9.8 G ion-steps/s against
+    // 28.7 / 11.1 / 6.4 with 3 everywhere). Wide records only in the first class: they win where
+    // the reloads hit L2 and lose where they reach HBM.
     const double rec = 48.0 * (double)nodes;
     t.blocks_per_sm = rec < 1.0e9 ? 3 : (rec < 4.0e9 ? 2 : 1);
+    t.wide = rec < 1.0e9 ? 1 : 0;
     return t;
 }
 
@@ -604,33 +628,38 @@ static cudaError_t enqueue_launches(const Scratch& s, const Tuning& t, const Mix
         const uint32_t ch = (L + 1 == launches) ? last_chunk : chunk;
         const uint32_t* li = lists + (size_t)in * n;
         uint32_t* lo = lists + (size_t)(in ^ 1) * n;
+        decltype(&k_mixed<true, true, true>) kern;
         if (mb.legacy_coll) {
-            if (t.prefetch) k_mixed<true, true><<<grid, t.tpb, 0, st>>>(nodes, mb, jobs, io, li, lo, ctr, in, ch, keep, kph, n);
-            else k_mixed<true, false><<<grid, t.tpb, 0, st>>>(nodes, mb, jobs, io, li, lo, ctr, in, ch, keep, kph, n);
+            if (t.wide) kern = t.prefetch ? k_mixed<true, true, true> : k_mixed<true, false, true>;
+            else kern = t.prefetch ? k_mixed<true, true, false> : k_mixed<true, false, false>;
         } else {
-            if (t.prefetch) k_mixed<false, true><<<grid, t.tpb, 0, st>>>(nodes, mb, jobs, io, li, lo, ctr, in, ch, keep, kph, n);
-            else k_mixed<false, false><<<grid, t.tpb, 0, st>>>(nodes, mb, jobs, io, li, lo, ctr, in, ch, keep, kph, n);
+            if (t.wide) kern = t.prefetch ? k_mixed<false, true, true> : k_mixed<false, false, true>;
+            else kern = t.prefetch ? k_mixed<false, true, false> : k_mixed<false, false, false>;
         }
+        kern<<<grid, t.tpb, 0, st>>>(nodes, mb, jobs, io, li, lo, ctr, in, ch, keep, kph, n);
         *kernels += 2;
     }
     return cudaGetLastError();
 }
 
-cudaError_t pack_nodes(Scratch& s, DevGrid g, uint64_t grid_gen, cudaStream_t st, uint32_t* kernels) {
-    if (s.nodes && s.nodes_gen == grid_gen) return cudaSuccess;
+cudaError_t pack_nodes(Scratch& s, DevGrid g, uint64_t grid_gen, int wide, cudaStream_t st, uint32_t* kernels) {
+    const int stride = wide ? 4 : 3;
+    if (s.nodes && s.nodes_gen == grid_gen && s.nodes_stride == stride) return cudaSuccess;
     cudaError_t e;
     const size_t n = (size_t)g.nx * g.ny * g.nz;
-    const size_t bytes = 3 * n * sizeof(float4);
+    const size_t bytes = (size_t)stride * n * sizeof(float4);
     if (s.nodes_cap < bytes) {
         if (s.nodes) cudaFree(s.nodes);
         s.nodes = nullptr; s.nodes_cap = 0;
         if ((e = cudaMalloc(&s.nodes, bytes)) != cudaSuccess) return e;
         s.nodes_cap = bytes;
     }
-    k_pack_nodes<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(g.rf, g.dc, g.ac, static_cast<float4*>(s.nodes), n, g.nx, g.ny, g.nz);
+    k_pack_nodes<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(g.rf, g.dc, g.ac, static_cast<float4*>(s.nodes), n, g.nx, g.ny, g.nz,
+                                                              stride);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     *kernels += 1;
     s.nodes_gen = grid_gen;
+    s.nodes_stride = stride;
     return cudaSuccess;
 }
 
@@ -640,7 +669,7 @@ cudaError_t run(Scratch& s, const Tuning& t, DevGrid g, uint64_t grid_gen, const
     *info = RunInfo();
     if (n == 0) return cudaSuccess;
     if (t.tpb != 128) return cudaErrorInvalidValue;   // the kernel is compiled for 128-thread blocks
-    if ((e = pack_nodes(s, g, grid_gen, st, &info->kernel_launches)) != cudaSuccess) return e;
+    if ((e = pack_nodes(s, g, grid_gen, t.wide, st, &info->kernel_launches)) != cudaSuccess) return e;
     const size_t list_bytes = (size_t)2 * n * sizeof(uint32_t);
     if (s.list_cap < list_bytes) {
         if (s.lists) cudaFree(s.lists);
@@ -687,7 +716,8 @@ cudaError_t run(Scratch& s, const Tuning& t, DevGrid g, uint64_t grid_gen, const
     const bool graph = t.use_graph && launches > 1;
     if (graph) {
         const uint64_t key[6] = {(uint64_t)(uintptr_t)s.lists, (uint64_t)n, launches, ((uint64_t)chunk << 32) | last_chunk,
-                                 (uint64_t)(uintptr_t)io.x ^ ((uint64_t)t.blocks_per_sm << 56) ^ ((uint64_t)t.prefetch << 60),
+                                 (uint64_t)(uintptr_t)io.x ^ ((uint64_t)t.blocks_per_sm << 56) ^ ((uint64_t)t.prefetch << 60) ^
+                                     ((uint64_t)t.wide << 61),
                                  (uint64_t)(uintptr_t)s.nodes ^ ((uint64_t)mb.legacy_coll << 62)};
         cudaGraph_t gr = nullptr;
         if ((e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return e;

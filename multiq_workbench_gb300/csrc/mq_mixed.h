@@ -43,6 +43,7 @@ struct Tuning {
     uint32_t chunk = 20000;    // steps per ion per launch (compaction interval)
     int use_graph = 1;         // replay the launch sequence as one CUDA graph
     int prefetch = 0;          // L1-prefetch the cell an ion is heading for
+    int wide = 0;              // 64-byte node records read with 256-bit loads (else 48-byte records)
     uint32_t max_launches = 0; // cap on launches per call (0 = as many as the step budget needs)
     int sms = 0;               // filled from the device
 };
@@ -56,9 +57,10 @@ struct Scratch {
     size_t jobs_cap = 0;
     void* keep = nullptr;      // working state of the call's ions (phase offsets, double-floats, staged flags)
     size_t keep_cap = 0;
-    void* nodes = nullptr;     // interleaved RF | DC | AC node records (float4 x 3 per node)
+    void* nodes = nullptr;     // interleaved RF | DC | AC node records (float4 x 3 or 4 per node)
     size_t nodes_cap = 0;
     uint64_t nodes_gen = ~0ull; // grid generation the records were packed from
+    int nodes_stride = 0;       // float4 per record of the packed records
     cudaGraphExec_t graph = nullptr;
     uint64_t graph_key[6] = {0, 0, 0, 0, 0, 0};
     cudaEvent_t ev[2] = {nullptr, nullptr};

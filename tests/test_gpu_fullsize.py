@@ -121,6 +121,7 @@ def test_default_shape_follows_the_grid_size(built):
         f = mq.Fields.build(mq.Geom.with_spacing(h), bases=[0, 1, 3, 4], cache=False, device=0)
         with mq.Engine(f, mq.PREC_MIXED) as e:
             assert e.tuning()["blocks_per_sm"] == want, h
+            assert not e.tuning()["wide_records"], h   # 48-byte records beyond 1 GB
             out = e.run_batch(jobs, [0.0, 5.0, -5.0, 0.0], ph)
             assert int(out.n.sum()) == 8000
         del f

@@ -131,6 +131,28 @@ def test_mixed_deterministic(coarse):
     _assert_bitequal(a, b, "mixed run twice")
 
 
+def test_record_widths_agree_bitwise(coarse):
+    """48-byte node records (128-bit loads) and 64-byte ones (256-bit loads) hold the same
+    values: per-ion results agree bit for bit, with and without the L1 prefetch, and switching
+    the width re-packs the records on the next call."""
+    mq = _mq()
+    ph = _variants()["half_kick_gauss"]
+    jobs = _jobs(512)
+    dc = [0.0, 5.0, -5.0, 0.0]
+    with mq.Engine(coarse, mq.PREC_MIXED) as e:
+        assert e.tuning()["wide_records"]          # the default below 1 GB of 48-byte records
+        a, _ = e.run_batch_ions(jobs, dc, ph)
+        e.set_tuning(wide_records=False)
+        b, _ = e.run_batch_ions(jobs, dc, ph)
+        e.set_tuning(prefetch=True)
+        c, _ = e.run_batch_ions(jobs, dc, ph)
+        e.set_tuning(wide_records=True)
+        d, _ = e.run_batch_ions(jobs, dc, ph)
+    _assert_bitequal(a, b, "wide vs narrow records")
+    _assert_bitequal(a, c, "wide vs narrow records with prefetch")
+    _assert_bitequal(a, d, "wide records with prefetch")
+
+
 def test_ragged_and_empty_jobs(coarse):
     """Jobs of 1, 0, 33, 2, 255 and 64 ions in one batch: the FP64 kernel's states equal the
     oracle's bit for bit, both engines count every job's ions once (the empty job included), and
