@@ -562,7 +562,8 @@ mq_status mq_run_batch(mq_engine* e, const mq_job* jobs, size_t njobs, const dou
     if ((s = upload_jobs(e, jobs, njobs, *ph, b, true, &tlen, &ntab, &h2d)) != MQ_OK) return s;
     mqd::JobTable jt;
     jt.jc = e->jobc.as<JobC>(); jt.first = e->jfirst.as<uint64_t>(); jt.seed = e->jseed.as<uint64_t>(); jt.njobs = (uint32_t)njobs;
-    CK(mqd::launch_inject(b, jt, dev_ions(e), (uint32_t)n, e->st), "inject kernel");
+    if (e->prec == MQ_PREC_F64) CK(mqd::launch_inject(b, jt, dev_ions(e), (uint32_t)n, e->st), "inject kernel");
+    else CK(mqmix::launch_inject(b, jt, dev_ions(e), (uint32_t)n, e->st), "inject kernel");
     uint64_t steps = 0;
     if (e->prec == MQ_PREC_F64) s = run_f64(e, b, tlen, n, 0xFFFFFFFFu, stats, &steps);
     else s = run_mixed(e, jobs, njobs, *ph, b, n, 0xFFFFFFFFu, ions_out ? 1 : 0, stats, &steps);

@@ -467,6 +467,101 @@ __global__ void k_pack_nodes(const float4* __restrict__ rf, const float4* __rest
     nodes[stride * q + 2] = ac[q];
 }
 
+// ---------------------------------------------------------------- injection for the mixed engine
+// The draws of mqp::inject_one (Ion::inject, world.rs:407-422, with chsim's launches,
+// channel.rs:342-366): the same seed, the same xorshift stream in the same order, so the ion's
+// generator state and its RF / AC phases are the FP64 injection's bit for bit; the transforms of
+// the draws (sqrt, log, sin / cos) run in FP32, as the reference's GPU path consumes FP32 ion
+// states (its injection runs on the host, channel.rs:342-366, and is narrowed to f32 for the
+// device). Positions take their FP32 offset from the axis in FP64, so they keep the axis exactly.
+// GB300's FP64 pipe makes the FP64 transforms (about 360 FP64 operations per ion) the whole cost
+// of the FP64 kernel k_inject; here an ion costs a few dozen FP32 operations.
+__device__ __forceinline__ uint64_t xs_raw(uint64_t* st) {   // xorshift64 step, world.rs:386-392
+    uint64_t x = *st;
+    x ^= x << 13;
+    x ^= x >> 7;
+    x ^= x << 17;
+    *st = x;
+    return x;
+}
+// (x >> 11) / 2^53 as FP32: top 24 bits plus the next 29 scaled below them (within 1 ulp)
+__device__ __forceinline__ float u53f(uint64_t x) {
+    return fmaf((float)((uint32_t)(x >> 11) & 0x1FFFFFFFu), 0x1.0p-53f, (float)(uint32_t)(x >> 40) * 0x1.0p-24f);
+}
+__device__ __forceinline__ double u53d(uint64_t x) { return (double)(x >> 11) * 0x1.0p-53; }   // exact
+// -ln u for u = (x >> 11) / 2^53 > 0, to FP32 accuracy also near u = 1, where 1 - u is formed
+// exactly in integers and the logarithm taken as log1p(-(1 - u))
+__device__ __forceinline__ float neg_log_u(uint64_t x) {
+    const uint64_t k = x >> 11;
+    if (k >= (1ull << 52)) return -log1pf(-(float)((1ull << 53) - k) * 0x1.0p-53f);
+    return -logf(u53f(x));
+}
+// sqrt(-2 ln max(u, 1e-300)): the FP64 clamp lies below FP32's range; only u = 0 reaches it
+__device__ __forceinline__ float gauss_radius(uint64_t x) {
+    return (x >> 11) ? sqrtf(2.0f * neg_log_u(x)) : 37.1692219f;
+}
+
+__global__ void __launch_bounds__(128) k_inject_mixed(mqp::Batch b, mqd::JobTable jt, DevIons io, uint32_t n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t lo = 0, hi = jt.njobs;   // the job of ion i: last job with first <= i
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (jt.first[mid] <= i) lo = mid; else hi = mid;
+    }
+    const mqp::JobC& j = jt.jc[lo];
+    uint64_t st = mqp::splitmix(jt.seed[lo] + ((uint64_t)i - jt.first[lo]) * 0x9E37ull) | 1ull;
+    float ox, oy, v0, v1, v2;
+    if (b.launch == 1) {               // legacy launch, channel.rs:350-355
+        const float kin = 0.1f * (0.75f + 0.75f * u53f(xs_raw(&st))) * (float)j.zc;
+        const float vin = sqrtf(2.0f * kin * ((float)mqp::QE / (float)j.m));
+        const float ang = (-10.0f + 20.0f * u53f(xs_raw(&st))) * (3.14159265f / 180.0f);
+        float sa, ca;
+        sincosf(ang, &sa, &ca);
+        ox = oy = 0.0f;
+        v0 = v1 = 0.707f * vin * sa;
+        v2 = vin * ca;
+    } else {
+        if (b.launch == 2) {           // Gaussian spot
+            const float r0 = gauss_radius(xs_raw(&st));
+            const float c0 = cospif(2.0f * u53f(xs_raw(&st)));
+            const float r1 = gauss_radius(xs_raw(&st));
+            const float c1 = cospif(2.0f * u53f(xs_raw(&st)));
+            ox = (float)b.sigma * r0 * c0;
+            oy = (float)b.sigma * r1 * c1;
+        } else {                       // uniform disc
+            const float r = (float)b.r_inject * sqrtf(u53f(xs_raw(&st)));
+            float sn, cs;
+            sincospif(2.0f * u53f(xs_raw(&st)), &sn, &cs);
+            ox = r * cs;
+            oy = r * sn;
+        }
+        const float s_ion = (float)j.s_ion;
+        const float ra = gauss_radius(xs_raw(&st));
+        const float ca = cospif(2.0f * u53f(xs_raw(&st)));
+        const float rb = gauss_radius(xs_raw(&st));
+        const float cb = cospif(2.0f * u53f(xs_raw(&st)));
+        v0 = s_ion * ra * ca;
+        v1 = s_ion * rb * cb;
+        v2 = s_ion * gauss_radius(xs_raw(&st));
+    }
+    const double ph_ac = u53d(xs_raw(&st));
+    const double prf = u53d(xs_raw(&st));
+    const uint64_t xf = xs_raw(&st);
+    // first free path -ln max(u, 1e-7) * mfp / 10 (channel.rs:365-366) as a step count; u < 1e-7
+    // exactly when (x >> 11) <= 900719925
+    const float nl = (xf >> 11) <= 900719925ull ? 16.1180957f : neg_log_u(xf);
+    const float first = nl * (float)j.mfp_mean / 10.0f;
+    const float vmag = sqrtf(fmaf(v0, v0, fmaf(v1, v1, v2 * v2)));
+    const float s0 = floorf(first / vmag / (float)b.dt) + 1.0f;
+    io.x[i] = b.a + (double)ox; io.y[i] = b.a + (double)oy; io.z[i] = b.z_inject;
+    io.vx[i] = (double)v0; io.vy[i] = (double)v1; io.vz[i] = (double)v2;
+    io.ph_rf[i] = b.rf_phase0 ? 0.0 : prf; io.ph_ac[i] = ph_ac;
+    io.rng[i] = st | 1ull;
+    io.leg[i] = s0 < 2147483520.0f ? (int32_t)s0 : 2147483647;
+    io.steps[i] = 0; io.ncoll[i] = 0; io.status[i] = 0; io.jid[i] = lo;
+}
+
 // initial live list (ions with status 0, warp-ballot compaction) and their working state: the
 // FP64 position / velocity in grid units as double-floats and the phase offsets as fixed-point
 // turns, converted here with every lane of a warp busy instead of one lane at a time in k_mixed
@@ -532,6 +627,12 @@ uint64_t fix64(double turns_per_step) {   // round(frac(w) * 2^64)
 }
 
 }  // namespace
+
+cudaError_t launch_inject(const mqp::Batch& b, mqd::JobTable jt, DevIons io, uint32_t n, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    k_inject_mixed<<<(n + 127) / 128, 128, 0, st>>>(b, jt, io, n);
+    return cudaGetLastError();
+}
 
 MixJob make_mix_job(const mqp::JobC& j, const mqp::Batch& b) {
     MixJob m;

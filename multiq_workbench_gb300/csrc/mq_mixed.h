@@ -78,6 +78,8 @@ struct RunInfo {
 
 MixJob make_mix_job(const mqp::JobC& j, const mqp::Batch& b);
 MixBatch make_mix_batch(const mqp::Batch& b);
+// device injection of a batch for the mixed engine: the FP64 injection's draws with FP32 transforms
+cudaError_t launch_inject(const mqp::Batch& b, mqd::JobTable jt, mqd::DevIons io, uint32_t n, cudaStream_t st);
 Tuning default_tuning(int device, size_t nodes);
 // write_states = 0 leaves the FP64 position / velocity of the ion states as they were (a caller
 // that wants only the counters, steps, status and collision counts)

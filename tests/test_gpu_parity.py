@@ -153,6 +153,34 @@ def test_record_widths_agree_bitwise(coarse):
     _assert_bitequal(a, d, "wide records with prefetch")
 
 
+@pytest.mark.parametrize("name", ["corrected_disc", "half_kick_gauss", "legacy_all"])
+def test_mixed_injection_draws(coarse, name):
+    """The mixed engine's device injection (a batch of zero steps returns it) makes the FP64
+    injection's draws: generator state, job, phases and counters equal bit for bit; from the
+    FP32 transforms, positions within 1e-5 cell, velocities within 4e-6 of |v| + the batch's median
+    |v| (an FP32 angle carries ~1e-7 absolute error, however slow the ion), and the
+    first-collision step count within 1e-5 relative (or 1 step)."""
+    import dataclasses
+    mq = _mq()
+    ph = dataclasses.replace(_variants()[name], t_max=0.0)
+    jobs = _jobs(700, legacy_species=(name == "legacy_all"))
+    n = sum(j.n for j in jobs)
+    with mq.Engine(coarse, mq.PREC_MIXED) as e:
+        ref = e.inject(jobs, ph)
+        got = mq.IonStates.empty(n)
+        out = e.run_batch(jobs, [0.0, 5.0, -5.0, 0.0], ph, ions_out=got)
+    assert sum(o.n for o in out) == n
+    for k in ("z", "ph_rf", "ph_ac", "rng", "steps", "ncoll", "status", "jid"):
+        assert np.array_equal(getattr(got, k), getattr(ref, k)), k
+    h = coarse.h
+    assert np.abs(got.pos() - ref.pos()).max() <= 1e-5 * h
+    vr, vg = ref.vel(), got.vel()
+    vn = np.linalg.norm(vr, axis=1)
+    assert (np.linalg.norm(vg - vr, axis=1) <= 4e-6 * (vn + np.median(vn))).all()
+    lr, lg = ref.leg.astype(np.float64), got.leg.astype(np.float64)
+    assert (np.abs(lg - lr) <= np.maximum(1e-5 * lr, 1.0)).all()
+
+
 def test_ragged_and_empty_jobs(coarse):
     """Jobs of 1, 0, 33, 2, 255 and 64 ions in one batch: the FP64 kernel's states equal the
     oracle's bit for bit, both engines count every job's ions once (the empty job included), and
