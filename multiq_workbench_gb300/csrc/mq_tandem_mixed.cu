@@ -8,9 +8,11 @@
 //   * position and velocity are FP32 double-floats in grid units of the track's current region
 //     (cube grid in mm, or the port's grid); region changes convert through FP64 with
 //     trapsim's enter / leave arithmetic (lib.rs:338-385);
-//   * fields as interleaved node records: cube {RF, region DC} 32 B, port {RF, DC (+ gate
-//     bias on idle ports), AC} 48 B with the cell's conductor bits in a spare word; the 8
-//     corners of the track's cell are held in registers and reloaded on a cell change;
+//   * fields as interleaved node records: cube {RF, region DC} 32 B (one 256-bit load), port
+//     {RF, DC (+ gate bias on idle ports), AC} 48 B with the cell's conductor bits in a spare word
+//     (64-byte port records with 256-bit loads measured 28% slower: the port grids' reloads reach
+//     HBM and pay for the larger footprint); the 8 corners of the track's cell are held in
+//     registers and reloaded on a cell change;
 //   * drive values per global step from the FP64 engine's drive table, rounded to FP32; thermal
 //     collisions with Philox-4x32-10 keyed by the track key and the global step (all lanes
 //     share the global step, so the generator runs warp-uniformly);
@@ -215,6 +217,12 @@ __device__ __forceinline__ void region_consts(const TMConst& C, int reg, float q
     }
 }
 
+// 32 bytes from a 32-byte aligned address (ld.global.nc.v8.f32, sm_100 and later): two float4
+__device__ __forceinline__ void ld256(const float4* p, float4& a, float4& b) {
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w) : "l"(p));
+}
+
 // the cell of grid position x (clamped to the grid), reloading the cache when it changes; a change
 // is found on floored floats, and indices are formed only when one is seen
 __device__ __forceinline__ void cell_for(const RegK& k, int reg, const float xh[3], TCell& c) {
@@ -231,7 +239,8 @@ __device__ __forceinline__ void cell_for(const RegK& k, int reg, const float xh[
             for (int q = 0; q < 8; ++q) {
                 uint32_t o = 2u * (base + (uint32_t)(q & 1) + ((q & 2) ? sy : 0u) + ((q & 4) ? sz : 0u));
                 o = (uint32_t)MQ_CHK_SPAN(o, 2, 2 * (size_t)sz * (size_t)k.nz, MQ_SITE_TMX_CELL);
-                const float4 r = __ldg(k.rec + o), d = __ldg(k.rec + o + 1);
+                float4 r, d;
+                ld256(k.rec + o, r, d);   // a 32-byte cube record in one load (1.6% on the tandem)
                 c.R[0][q] = r.x; c.R[1][q] = r.y; c.R[2][q] = r.z;
                 c.D[0][q] = d.x; c.D[1][q] = d.y; c.D[2][q] = d.z;
             }
