@@ -100,9 +100,9 @@ __global__ void __launch_bounds__(128) k_f64_step(DevGrid g, Batch b, const JobC
                         q = MQ_CHK(q, nx * ny * (size_t)g.nz, MQ_SITE_F64_FIELD);
                         double w = wx * wy * wz;
                         float4 r = __ldg(g.rf + q), a = __ldg(g.ac + q), c = __ldg(g.dc + q);
-                        er[0] += w * (double)r.x; er[1] += w * (double)r.y; er[2] += w * (double)r.z;
-                        ea[0] += w * (double)a.x; ea[1] += w * (double)a.y; ea[2] += w * (double)a.z;
-                        ed[0] += w * (double)c.x; ed[1] += w * (double)c.y; ed[2] += w * (double)c.z;
+                        er[0] += w * mqp::widen(r.x); er[1] += w * mqp::widen(r.y); er[2] += w * mqp::widen(r.z);
+                        ea[0] += w * mqp::widen(a.x); ea[1] += w * mqp::widen(a.y); ea[2] += w * mqp::widen(a.z);
+                        ed[0] += w * mqp::widen(c.x); ed[1] += w * mqp::widen(c.y); ed[2] += w * mqp::widen(c.z);
                     }
                 }
             }

