@@ -113,7 +113,10 @@ mq_status   mq_inject_grid(const mq_grid_desc* grid, const mq_job* jobs, size_t 
 mq_status   mq_run_ions(mq_engine* e, const mq_job* jobs, size_t njobs, const mq_physics* ph, mq_ions* io, size_t n,
                         uint32_t max_more, mq_run_stats* stats);
 /* chsim run_batch: inject (on the device), run every ion to completion, count per job.
- * out[njobs] receives the outcomes; ions_out (may be NULL) receives final states. */
+ * out[njobs] receives the outcomes; ions_out (may be NULL) receives final states.  The FP64
+ * engine injects exactly as mq_inject; the mixed engine makes the same random draws (generator
+ * state, phases and counters identical) and transforms them to positions and velocities in FP32,
+ * the precision the reference's GPU path consumes them in. */
 mq_status   mq_run_batch(mq_engine* e, const mq_job* jobs, size_t njobs, const double dc[4], const mq_physics* ph,
                          mq_outcome* out, mq_ions* ions_out, mq_run_stats* stats);
 mq_status   mq_summarize(const mq_ions* io, size_t n, double dt, size_t njobs, mq_outcome* out);
