@@ -283,7 +283,7 @@ mq_status upload_jobs(mq_engine* e, const mq_job* jobs, size_t njobs, const mq_p
 mqd::DevGrid dev_grid(const mq_engine* e) {
     mqd::DevGrid g;
     g.rf = e->d_rf; g.ac = e->d_ac; g.dc = e->d_dc;
-    g.nx = e->nx; g.ny = e->ny; g.nz = e->nz; g.pad = 0; g.h = e->h;
+    g.nx = e->nx; g.ny = e->ny; g.nz = e->nz; g.pad = 0; g.h = e->h; g.inv_h = 1.0 / e->h;
     return g;
 }
 

@@ -13,6 +13,7 @@ struct DevGrid {
     const float4* dc;   // combined static DC
     int32_t nx, ny, nz, pad;
     double h;
+    double inv_h;       // 1 / h, correctly rounded (the FP64 kernel's division by h)
 };
 
 struct DevIons {        // device structure of arrays (FP64 state)

@@ -81,7 +81,7 @@ extern "C" mq_status mq_run_ions_device_noalloc(const mq_dev_grid* grid, const m
     g.rf = reinterpret_cast<const float4*>(grid->rf4);
     g.ac = reinterpret_cast<const float4*>(grid->ac4);
     g.dc = reinterpret_cast<const float4*>(grid->dc4);
-    g.nx = grid->nx; g.ny = grid->ny; g.nz = grid->nz; g.pad = 0; g.h = grid->h;
+    g.nx = grid->nx; g.ny = grid->ny; g.nz = grid->nz; g.pad = 0; g.h = grid->h; g.inv_h = 1.0 / grid->h;
     mqd::DevIons d;
     d.x = io->x; d.y = io->y; d.z = io->z; d.vx = io->vx; d.vy = io->vy; d.vz = io->vz;
     d.ph_rf = io->ph_rf; d.ph_ac = io->ph_ac; d.rng = io->rng; d.steps = io->steps; d.ncoll = io->ncoll;
