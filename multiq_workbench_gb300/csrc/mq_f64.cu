@@ -46,18 +46,6 @@ __global__ void k_phase_table(double w, uint32_t len, double2* out) {
     out[i] = make_double2(s, c);
 }
 
-// x / h correctly rounded without a division: q = x * RN(1/h), then one step of Markstein's correction
-// q + (x - q h) RN(1/h) with fused multiply-adds (P. Markstein, IBM J. Res. Dev. 34 (1990) 111-119:
-// with a correctly rounded reciprocal and a quotient within one ulp the corrected quotient is the
-// correctly rounded one, barring overflow and underflow, which positions in metres never reach).
-// The sign of a zero quotient is the dividend's, as in x / h with h > 0. Three FP64 operations in
-// place of the division's sequence on GB300's narrow FP64 pipe; checked against IEEE x / h on
-// 2.1e9 positions at 14 grid spacings, and bit for bit by the oracle parity tests.
-__device__ __forceinline__ double div_h(double x, double h, double inv_h) {
-    const double q = __dmul_rn(x, inv_h);
-    return copysign(fma(fma(-q, h, x), inv_h, q), x);
-}
-
 __device__ __forceinline__ void table_get(const double2* t, uint32_t tlen, double w, uint32_t n, double* s, double* c) {
     if (n < tlen) { double2 v = __ldg(t + n); *s = v.x; *c = v.y; }
     else mqp::phase_at(w, n, s, c);
@@ -94,7 +82,7 @@ __global__ void __launch_bounds__(128) k_f64_step(DevGrid g, Batch b, const JobC
                 sac = jc.v_ac * (Sa * ac + Ca * as_);
             }
             // fields_at: one pass over the 8 corners, weights (1-t, t) in order i, j, k
-            double gx = div_h(x[0], h, g.inv_h), gy = div_h(x[1], h, g.inv_h), gz = div_h(x[2], h, g.inv_h);
+            double gx = mqp::div_rn(x[0], h, g.inv_h), gy = mqp::div_rn(x[1], h, g.inv_h), gz = mqp::div_rn(x[2], h, g.inv_h);
             int32_t ci = mqp::cell_lo(gx, g.nx), cj = mqp::cell_lo(gy, g.ny), ck = mqp::cell_lo(gz, g.nz);
             double tx = gx - (double)ci, ty = gy - (double)cj, tz = gz - (double)ck;
             if (b.nearest) { tx = 0.0; ty = 0.0; tz = 0.0; }
@@ -177,8 +165,8 @@ __global__ void __launch_bounds__(128) k_f64_step(DevGrid g, Batch b, const JobC
             if (x[2] < b.z_return) { status = 2; break; }
             if (x[0] < 0.0 || x[1] < 0.0 || x[2] < 0.0 || x[0] > b.lim[0] || x[1] > b.lim[1] || x[2] > b.lim[2]) { status = 4; break; }
             if (x[2] > b.crash_z0 && x[2] < b.crash_z1) {
-                int32_t ni = mqp::node_round(div_h(x[0], h, g.inv_h), g.nx), nj = mqp::node_round(div_h(x[1], h, g.inv_h), g.ny),
-                        nk = mqp::node_round(div_h(x[2], h, g.inv_h), g.nz);
+                int32_t ni = mqp::node_round(mqp::div_rn(x[0], h, g.inv_h), g.nx), nj = mqp::node_round(mqp::div_rn(x[1], h, g.inv_h), g.ny),
+                        nk = mqp::node_round(mqp::div_rn(x[2], h, g.inv_h), g.nz);
                 size_t q = (size_t)ni + nx * ((size_t)nj + ny * (size_t)nk);
                 q = MQ_CHK(q, nx * ny * (size_t)g.nz, MQ_SITE_F64_CRASH);
                 if (__ldg(&g.rf[q].w) > 0.5f) { status = 1; break; }

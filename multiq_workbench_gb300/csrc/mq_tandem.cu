@@ -28,14 +28,14 @@ struct TSpec { double qmdt, s_ion, mr, nsd; };
 
 struct TPort {                  // one port's channel grid and drive
     int32_t kn[3], idle;
-    double kh, lim[3];
+    double kh, inv_kh, lim[3];   // spacing [m], its correctly rounded reciprocal, box limits
     const float4 *rf, *ac, *dc, *gate;
 };
 
 struct TConst {
     mq_cube_geom cube;
     int32_t cn[3];
-    double clo[3], ch_mm;
+    double clo[3], ch_mm, inv_ch_mm;
     const float4* crf;
     const float4* cdc[2];
     TPort port[9];
@@ -59,7 +59,7 @@ __device__ void cube_field(const TConst& C, const float4* dc, const double x[3],
     double w[3];
     for (int a = 0; a < 3; ++a) {
         const double p = x[a] * 1000.0;
-        const double f = clampd((p - C.clo[a]) / C.ch_mm, 0.0, (double)(C.cn[a] - 1) - 1e-9);
+        const double f = clampd(mqp::div_rn(p - C.clo[a], C.ch_mm, C.inv_ch_mm), 0.0, (double)(C.cn[a] - 1) - 1e-9);
         c[a] = f > 0.0 ? (int)floor(f) : 0;   // NaN -> 0 as Rust's `as usize`
         w[a] = f - (double)c[a];
     }
@@ -80,7 +80,7 @@ __device__ void cube_field(const TConst& C, const float4* dc, const double x[3],
 // channel fields_at (world.rs:265-288) and gate_delta (world.rs:291-302) on the port's grid
 __device__ void chan_field(const TPort& P, double gate_v, const double x[3], double rf, double ac, double e[3]) {
     const double h = P.kh;
-    const double g[3] = {x[0] / h, x[1] / h, x[2] / h};
+    const double g[3] = {mqp::div_rn(x[0], h, P.inv_kh), mqp::div_rn(x[1], h, P.inv_kh), mqp::div_rn(x[2], h, P.inv_kh)};
     const int32_t i0 = mqp::cell_lo(g[0], P.kn[0]), j0 = mqp::cell_lo(g[1], P.kn[1]), k0 = mqp::cell_lo(g[2], P.kn[2]);
     const double tx = g[0] - (double)i0, ty = g[1] - (double)j0, tz = g[2] - (double)k0;
     double er[3] = {0, 0, 0}, ea[3] = {0, 0, 0}, ed[3] = {0, 0, 0};
@@ -119,8 +119,9 @@ __device__ void chan_field(const TPort& P, double gate_v, const double x[3], dou
 __device__ bool chan_crash(const TPort& P, const double x[3]) {   // world.rs:309-314
     for (int d = 0; d < 3; ++d)
         if (x[d] < 0.0 || x[d] > P.lim[d]) return true;
-    const int32_t ni = mqp::node_round(x[0] / P.kh, P.kn[0]), nj = mqp::node_round(x[1] / P.kh, P.kn[1]),
-                  nk = mqp::node_round(x[2] / P.kh, P.kn[2]);
+    const int32_t ni = mqp::node_round(mqp::div_rn(x[0], P.kh, P.inv_kh), P.kn[0]),
+                  nj = mqp::node_round(mqp::div_rn(x[1], P.kh, P.inv_kh), P.kn[1]),
+                  nk = mqp::node_round(mqp::div_rn(x[2], P.kh, P.inv_kh), P.kn[2]);
     size_t q = (size_t)ni + (size_t)P.kn[0] * ((size_t)nj + (size_t)P.kn[1] * (size_t)nk);
     q = MQ_CHK(q, (size_t)P.kn[0] * (size_t)P.kn[1] * (size_t)P.kn[2], MQ_SITE_TDM_CRASH);
     return P.rf[q].w > 0.5f;
@@ -358,6 +359,7 @@ mq_status mq_tandem_create(const mq_tandem_desc* d, int32_t device, mq_tandem** 
             P.lim[a] = (double)(p.dims[a] - 1) * p.h;   // World::lim (world.rs:145)
         }
         P.kh = p.h;
+        P.inv_kh = 1.0 / p.h;
         P.idle = p.tone_khz == 0.0;
     }
     if (cudaMalloc(&t->counts, 9 * kNC * sizeof(uint32_t)) != cudaSuccess) return bail(MQ_ERR_NOMEM);
@@ -365,6 +367,7 @@ mq_status mq_tandem_create(const mq_tandem_desc* d, int32_t device, mq_tandem** 
     C.cube = d->cube;
     for (int a = 0; a < 3; ++a) { C.cn[a] = d->cube_dims[a]; C.clo[a] = d->cube_lo_mm[a]; }
     C.ch_mm = d->cube_h_mm;
+    C.inv_ch_mm = 1.0 / d->cube_h_mm;
     double mouths[18];
     mq_tandem_layout(d, &C.seam, &C.size, mouths);
     for (int i = 0; i < 9; ++i) { C.mouth[i][0] = mouths[2 * i]; C.mouth[i][1] = mouths[2 * i + 1]; }
