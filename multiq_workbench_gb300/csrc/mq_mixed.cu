@@ -10,13 +10,14 @@
 //   * positions in grid units and velocities in cells per step, each an FP32 double-float
 //     (compensated two-sum accumulator); field nodes, interpolation and collision
 //     kinematics in FP32;
-//   * fields as 64-byte interleaved node records; the 8 corners of the ion's cell x
-//     {RF, DC, AC} held in registers and reloaded only when the ion changes cell (the
-//     cached conductor bits of the corners give the nearest-node crash test), with an L1
-//     prefetch of the cell the ion is heading for;
+//   * fields as interleaved node records of 64 bytes (256-bit loads) or 48 bytes, by grid size;
+//     the 8 corners of the ion's cell x {RF, DC, AC} held in registers and reloaded only when
+//     the ion changes cell (the cached conductor bits of the corners give the nearest-node
+//     crash test), with an optional L1 prefetch of the cell the ion is heading for;
 //   * RF / AC phase as exact 64-bit fixed-point turn accumulators (phase = offset +
 //     step * f * dt mod 1), evaluated with an FP32 quarter-turn polynomial;
-//   * Philox-4x32-10 counter RNG keyed by the ion's 64-bit key, counter = step.
+//   * Philox-4x32-10 counter RNG keyed by the ion's 64-bit key, counter = step;
+//   * device injection with the FP64 injection's draws and FP32 transforms (k_inject_mixed).
 #include "mq_mixed.h"
 #include "mq_check.h"
 
