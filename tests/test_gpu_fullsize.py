@@ -6,7 +6,9 @@
   sampled jobs has the state it gets when its job runs alone; the mixed engine's outcome counts
   match the FP64 kernel's (which is bit-exact with the oracle) within binomial limits;
 * the tandem (1,048,576 tracks, nine 0.050 mm port grids): the region census conserves tracks
-  at every frame, the port counters balance, and a rerun gives the same bits.
+  at every frame, the port counters balance, and a rerun gives the same bits;
+* the grid study's 0.050 mm grid (49.6 M nodes): the FP64 kernel equals the oracle bit for bit on
+  a sample of its launch (the oracle replays a few hundred ions there in under a second).
 """
 import math
 
@@ -125,3 +127,28 @@ def test_default_shape_follows_the_grid_size(built):
             out = e.run_batch(jobs, [0.0, 5.0, -5.0, 0.0], ph)
             assert int(out.n.sum()) == 8000
         del f
+
+
+def test_f64_bitexact_vs_oracle_on_the_0p05_grid(built):
+    """Bit-exact FP64 parity at a large grid: on the 0.050 mm channel grid of the grid study
+    (320 x 320 x 484 = 49.6 M nodes, solved on the GPU) the FP64 kernel's final states of 2 jobs x
+    96 ions of the grid-study launch, run to completion, equal the oracle's in all 14 fields."""
+    import multiq_workbench_gb300 as mq
+    from oracle import mqref as R
+    f = mq.Fields.build(mq.Geom.with_spacing(0.05), bases=[0, 1, 3, 4], cache=False, device=0)
+    dc = [0.0, 5.0, -5.0, 0.0]
+    ph = mq.Physics(legacy_force=True, pressure_pa=0.133322, temp_k=300.0, dt=1e-7, t_max=20000 * 1e-7,
+                    launch=mq.LAUNCH_GAUSSIAN, sigma_mm=0.1)
+    drive = mq.RfAc(100.0, 500e3, 0.5, 100e3)
+    jobs = [mq.Job(mq.Species(499.0, 1.0, 2.95 * 499.0 ** (2.0 / 3.0)), drive, 96, s) for s in (11, 12)]
+    with mq.Engine(f, mq.PREC_F64) as e:
+        ions, _ = e.run_batch_ions(jobs, dc, ph)
+    g = f.geom
+    G = R.Grid3(f.nx, f.ny, f.nz, f.h, f.rf, f.ac, f.dc_field(dc))
+    b = R.batch(ph, drive.v_rf, drive.f_rf, g.axis(), g.layers())
+    s = R.inject(b, jobs, len(ions))
+    R.run(G, b, jobs, s)
+    assert int((s.status != 0).sum()) == len(ions)
+    for name, _ in R.FIELDS:
+        a, c = np.asarray(getattr(ions, name)), np.asarray(getattr(s, name))
+        assert np.array_equal(a.view(np.uint8), c.view(np.uint8)), name
