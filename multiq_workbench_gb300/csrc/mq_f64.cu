@@ -46,6 +46,34 @@ __global__ void k_phase_table(double w, uint32_t len, double2* out) {
     out[i] = make_double2(s, c);
 }
 
+// Comparisons and integer <-> double conversions of the step on the integer pipe. GB300's FP64 pipe
+// limits this kernel and also executes FP64 compares and conversions; these helpers give the same
+// results from the doubles' bit patterns (IEEE doubles of one sign order like their bits as
+// integers), NaN and signed zeros included.
+__device__ __forceinline__ bool is_nan_bits(long long b) { return (b & 0x7FFFFFFFFFFFFFFFLL) > 0x7FF0000000000000LL; }
+// x > c for a constant c > 0
+__device__ __forceinline__ bool gt_pos(long long x, long long c) { return x > c && x <= 0x7FF0000000000000LL; }
+// x < c for a constant c > 0 (negative numbers and -0 included, NaN excluded)
+__device__ __forceinline__ bool lt_pos(long long x, long long c) { return x < c && !is_nan_bits(x); }
+// x < 0
+__device__ __forceinline__ bool lt_zero(long long x) { return x < 0 && x != (long long)0x8000000000000000ULL && !is_nan_bits(x); }
+// mqp::cell_lo (clamp to [0, n - 2], truncate) from the bits of g; lim = the bits of (double)(n - 2)
+__device__ __forceinline__ int32_t cell_lo_bits(double g, int32_t n, long long lim) {
+    const long long b = __double_as_longlong(g);
+    if (b <= 0 || b > 0x7FF0000000000000LL) return 0;   // !(g > 0): zeros, negatives, NaN
+    if (b >= lim) return n - 2;                          // g >= n - 2, +inf included
+    const int e = (int)(b >> 52) - 1023;                 // 0 < g < n - 2 < 2^31
+    if (e < 0) return 0;
+    return (int32_t)(((b & 0xFFFFFFFFFFFFFLL) | 0x10000000000000LL) >> (52 - e));
+}
+// (double)v for 0 <= v < 2^31, exactly
+__device__ __forceinline__ double i2d_bits(int32_t v) {
+    if (v == 0) return 0.0;
+    const int e = 31 - __clz(v);
+    const unsigned long long m = ((unsigned long long)(uint32_t)v << (52 - e)) & 0xFFFFFFFFFFFFFULL;
+    return __longlong_as_double((long long)(((unsigned long long)(1023 + e) << 52) | m));
+}
+
 __device__ __forceinline__ void table_get(const double2* t, uint32_t tlen, double w, uint32_t n, double* s, double* c) {
     if (n < tlen) { double2 v = __ldg(t + n); *s = v.x; *c = v.y; }
     else mqp::phase_at(w, n, s, c);
@@ -71,6 +99,12 @@ __global__ void __launch_bounds__(128) k_f64_step(DevGrid g, Batch b, const JobC
         mqp::sincos2pi(io.ph_rf[i], &rs, &rc);
         mqp::sincos2pi(io.ph_ac[i], &as_, &ac);
         const double dt = b.dt, qmdt = jc.qmdt, h = g.h;
+        // bit patterns of the step's positive thresholds for the integer-pipe comparisons
+        const long long lim_x = __double_as_longlong((double)(g.nx - 2)), lim_y = __double_as_longlong((double)(g.ny - 2)),
+                        lim_z = __double_as_longlong((double)(g.nz - 2));
+        const long long k_exit = __double_as_longlong(b.z_exit), k_return = __double_as_longlong(b.z_return);
+        const long long k_lim0 = __double_as_longlong(b.lim[0]), k_lim1 = __double_as_longlong(b.lim[1]),
+                        k_lim2 = __double_as_longlong(b.lim[2]);
         const size_t nx = (size_t)g.nx, ny = (size_t)g.ny;
         while (done < max_more) {
             double S, Cc, Sa = 0.0, Ca = 0.0;
@@ -83,8 +117,8 @@ __global__ void __launch_bounds__(128) k_f64_step(DevGrid g, Batch b, const JobC
             }
             // fields_at: one pass over the 8 corners, weights (1-t, t) in order i, j, k
             double gx = mqp::div_rn(x[0], h, g.inv_h), gy = mqp::div_rn(x[1], h, g.inv_h), gz = mqp::div_rn(x[2], h, g.inv_h);
-            int32_t ci = mqp::cell_lo(gx, g.nx), cj = mqp::cell_lo(gy, g.ny), ck = mqp::cell_lo(gz, g.nz);
-            double tx = gx - (double)ci, ty = gy - (double)cj, tz = gz - (double)ck;
+            int32_t ci = cell_lo_bits(gx, g.nx, lim_x), cj = cell_lo_bits(gy, g.ny, lim_y), ck = cell_lo_bits(gz, g.nz, lim_z);
+            double tx = gx - i2d_bits(ci), ty = gy - i2d_bits(cj), tz = gz - i2d_bits(ck);
             if (b.nearest) { tx = 0.0; ty = 0.0; tz = 0.0; }
             double er[3] = {0.0, 0.0, 0.0}, ea[3] = {0.0, 0.0, 0.0}, ed[3] = {0.0, 0.0, 0.0};
 #pragma unroll
@@ -161,9 +195,13 @@ __global__ void __launch_bounds__(128) k_f64_step(DevGrid g, Batch b, const JobC
                     leg = !(st < 2147483647.0) ? 2147483647 : (int32_t)st;
                 }
             }
-            if (x[2] > b.z_exit) { status = 3; break; }
-            if (x[2] < b.z_return) { status = 2; break; }
-            if (x[0] < 0.0 || x[1] < 0.0 || x[2] < 0.0 || x[0] > b.lim[0] || x[1] > b.lim[1] || x[2] > b.lim[2]) { status = 4; break; }
+            const long long bx = __double_as_longlong(x[0]), by = __double_as_longlong(x[1]), bz = __double_as_longlong(x[2]);
+            if (gt_pos(bz, k_exit)) { status = 3; break; }
+            if (lt_pos(bz, k_return)) { status = 2; break; }
+            if (lt_zero(bx) || lt_zero(by) || lt_zero(bz) || gt_pos(bx, k_lim0) || gt_pos(by, k_lim1) || gt_pos(bz, k_lim2)) {
+                status = 4;
+                break;
+            }
             if (x[2] > b.crash_z0 && x[2] < b.crash_z1) {
                 int32_t ni = mqp::node_round(mqp::div_rn(x[0], h, g.inv_h), g.nx), nj = mqp::node_round(mqp::div_rn(x[1], h, g.inv_h), g.ny),
                         nk = mqp::node_round(mqp::div_rn(x[2], h, g.inv_h), g.nz);
