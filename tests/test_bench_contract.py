@@ -10,7 +10,7 @@ from pathlib import Path
 ROOT = Path(__file__).resolve().parents[1]
 
 
-def test_reference_arm_json_line():
+def test_reference_arm_json_line(built):
     out = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "1", "--warmup", "0"],
                          cwd=ROOT, check=True, capture_output=True, text=True, timeout=600).stdout
     lines = [l for l in out.splitlines() if l.startswith("{")]
