@@ -35,7 +35,37 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "ion-steps/s, 1 GB300: batched mixed-precision vs plain FP64 at matched outcomes"
 UNIT = "ion-steps/s"
-BYTES_PER_ION_STEP = 384   # 8 corner nodes x 3 float4 fields (RF+mask, DC, AC) x 16 B
+# Bytes the stepping kernel must move, counted by the kernel itself: every cell-cache fill reads the
+# 8 corner node records of a cell (64 or 48 B each), and every ion it takes from the queue reads its
+# working state and job constants and writes them back (ION_STATE_BYTES).  The 384 B of corner
+# values an ion-step interpolates (8 corners x 3 float4) come from registers between fills.
+CORNERS = 8
+ION_STATE_BYTES = 48 + 16 + 24 + 56 + 64   # double-floats, phase offsets, counters + key, job record; write-back
+
+
+def stepping_bytes(stats, wide: bool) -> float:
+    """Algorithmic bytes of the stepping kernel(s) of one call, from the kernel's own counters: cell
+    fills x 8 node records, plus the state traffic of every ion taken from the work queue."""
+    rec = 64 if wide else 48
+    return float(stats.cell_loads) * CORNERS * rec + float(stats.ions_queued) * ION_STATE_BYTES
+
+
+def cpu_model() -> str:
+    """The host CPU's model name (/proc/cpuinfo, else lscpu), for the CPU baseline's line."""
+    try:
+        for line in Path("/proc/cpuinfo").read_text().splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return "unknown"
 
 
 def workload(ions_per_job: int = 256, seed0: int = 0):
@@ -119,6 +149,8 @@ def run_gridstudy(args, rank: int, world: int):
                 ms.append(eng.last_stats.kernel_ms)
                 steps = eng.last_stats.ion_steps
             step_ms = eng.last_stats.step_kernel_ms
+            moved = stepping_bytes(eng.last_stats, tuned["wide_records"])
+            loads_per_step = eng.last_stats.cell_loads / max(steps, 1)
             ions_m = mq.IonStates.empty(n)
             om = eng.run_batch(table, dc, ph, ions_out=ions_m)
         rate = steps / (float(np.mean(ms)) * 1e-3)
@@ -128,11 +160,10 @@ def run_gridstudy(args, rank: int, world: int):
                 ions_d = mq.IonStates.empty(n)
                 o64 = e64.run_batch(table, dc, ph, ions_out=ions_d)
                 s64 = e64.last_stats
-            cls = {k: (int(getattr(om, k).sum()), int(getattr(o64, k).sum())) for k in ("returned", "crashed", "left",
-                                                                                     "transmitted", "timeout")}
-            for k, (a, b) in cls.items():
-                p = (a + b + 1) / (2 * n + 2)
-                pulls[k] = {"mixed": a, "fp64": b, "pull": (a - b) / math.sqrt(2 * n * p * (1 - p))}
+            from multiq_workbench_gb300 import validate as V
+            cmp = V.compare_classes(V.class_counts(om), V.class_counts(o64))
+            pulls = {"chi2": cmp["chi2"], "dof": cmp["dof"], "p": cmp["p"],
+                     "classes": {k: {"mixed": c["a"], "fp64": c["b"], "pull": c["pull"]} for k, c in cmp["classes"].items()}}
             agree = float(np.mean(ions_m.status == ions_d.status))
         nodes = f.nx * f.ny * f.nz
         grids.append({"h_mm": h, "dims": [f.nx, f.ny, f.nz], "nodes": nodes,
@@ -140,9 +171,10 @@ def run_gridstudy(args, rank: int, world: int):
                       "tuning": tuned,
                       "mixed": {"value": rate, "unit": UNIT, "ms_per_step": float(np.mean(ms)),
                                 "e2e": steps / float(np.mean(walls)), "ion_steps": int(steps),
-                                "roofline_frac": BYTES_PER_ION_STEP * steps / (step_ms * 1e-3) / 1e9 / hbm,
-                                "roofline_l2_frac": (BYTES_PER_ION_STEP * steps / (step_ms * 1e-3) / 1e9 / l2)
-                                if l2 else None},
+                                "cell_loads_per_ion_step": loads_per_step,
+                                "achieved_gbs": moved / (step_ms * 1e-3) / 1e9,
+                                "roofline_frac": moved / (step_ms * 1e-3) / 1e9 / hbm,
+                                "roofline_l2_frac": (moved / (step_ms * 1e-3) / 1e9 / l2) if l2 else None},
                       "fp64_gpu": {"value": s64.ion_steps / (s64.kernel_ms * 1e-3), "unit": UNIT} if s64 else None,
                       "counts": pulls,
                       "class_agreement": agree})
@@ -161,11 +193,14 @@ def run_gridstudy(args, rank: int, world: int):
             "e2e": {"value": fin["mixed"]["e2e"], "unit": UNIT, "h2d_bytes_per_step": int(table.arr.nbytes),
                     "d2h_bytes_per_step": int(len(jobs) * 64)},
             "gpu_launches": None,
-            "roofline": {"bound": "hbm", "achieved": fin["mixed"]["roofline_frac"] * hbm, "peak": hbm, "unit": "GB/s",
+            "roofline": {"bound": "hbm", "achieved": fin["mixed"]["achieved_gbs"], "peak": hbm, "unit": "GB/s",
                          "frac": fin["mixed"]["roofline_frac"], "traffic": None,
                          "peak_source": "measured hbm_gbs" if peaks.get("hbm_gbs") else "fallback",
-                         "kernel": "k_mixed", "algorithmic_bytes_per_ion_step": BYTES_PER_ION_STEP},
-            "roofline_l2": {"achieved": fin["mixed"]["roofline_frac"] * hbm, "peak": l2, "unit": "GB/s",
+                         "kernel": "k_mixed",
+                         "algorithmic_bytes": "cell fills counted by the kernel x 8 node records (48 B) + "
+                                              f"{ION_STATE_BYTES} B per ion taken from the queue",
+                         "cell_loads_per_ion_step": fin["mixed"]["cell_loads_per_ion_step"]},
+            "roofline_l2": {"achieved": fin["mixed"]["achieved_gbs"], "peak": l2, "unit": "GB/s",
                             "frac": fin["mixed"]["roofline_l2_frac"],
                             "peak_source": "L2 read bandwidth measured in this run (mq_measure_l2_read_gbs)"},
             "cpu_baseline": None, "clocks": clk, "grids": grids}
@@ -317,7 +352,7 @@ def run_reference(args, rank: int, world: int):
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": "batched sweep 64 f_ac x 8 V_ac x 32 m/z x 256 ions (4,194,304 ions), 0.100 mm grid, legacy half-kick",
                        "sample": f"{r['jobs']} of the 16384 jobs, evenly spaced, all their ions: {r['ions']} ions per step"},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "cpu": cpu_model(), "kind": "port",
                              "sample": f"{r['ions']} ions of {r['jobs']} evenly spaced jobs, run to completion"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -355,16 +390,6 @@ def tandem_setup(args, rank: int = 0, precision: int = 1, grids=None):
 def tandem_bytes(st, kind: str = "mixed") -> float:
     b = TANDEM_BYTES[kind]
     return b["cube"] * st.steps_cube + b["port"] * st.steps_port + b["idle"] * st.steps_idle
-
-
-def tandem_traffic():
-    """DRAM bytes of one full-size k_tm_step launch (256 steps) from the committed ncu summary."""
-    import re
-    prof = ROOT / "profiles" / "k_tm_step_tandem.md"
-    if not prof.exists():
-        return None
-    m = re.search(r"dram_bytes_per_launch:\s*([0-9.eE+]+)", prof.read_text())
-    return float(m.group(1)) if m else None
 
 
 def tandem_cpu(m, pulse, steps: int, target_s: float, threads: int) -> dict:
@@ -409,7 +434,8 @@ def run_tandem(args, rank: int, world: int):
                           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall / max(1, args.steps),
                           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                           "data": "synthetic", "config": {"workload": wl, "sample": smp},
-                          "cpu_baseline": {"value": v, "unit": TANDEM_UNIT, "cores": threads, "kind": "port", "sample": smp},
+                          "cpu_baseline": {"value": v, "unit": TANDEM_UNIT, "cores": threads, "cpu": cpu_model(), "kind": "port",
+                                           "sample": smp},
                           "e2e": {"value": v, "unit": TANDEM_UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}),
               flush=True)
         return
@@ -482,12 +508,13 @@ def run_tandem(args, rank: int, world: int):
             cmp[name] = {"mixed": int(a), "fp64": int(b), "pull": pull(float(a), float(b))}
         extra["fp64_gpu"] = {"value": s64.track_steps / (s64.kernel_ms * 1e-3), "unit": TANDEM_UNIT,
                              "speedup_mixed_over_fp64": (ts / t_dev) / (s64.track_steps / (s64.kernel_ms * 1e-3)),
+                             "fp64_note": "GB300's FP64 rate is a small fraction of its FP32 rate, which the ratio reflects",
                              "roofline_achieved_gbs": tandem_bytes(s64, "f64") / (s64.kernel_ms * 1e-3) / 1e9,
                              "sample": "the same pulse and steps", "counts": cmp}
     cpu = None
     if not args.no_cpu:
         r = tandem_cpu(m, pulse, args.tandem_steps, 12.0, threads)
-        cpu = {"value": r["value"], "unit": TANDEM_UNIT, "cores": threads, "kind": "port",
+        cpu = {"value": r["value"], "unit": TANDEM_UNIT, "cores": threads, "cpu": cpu_model(), "kind": "port",
                "sample": f"first {r['tracks']} tracks of the pulse for {args.tandem_steps} steps ({r['seconds']:.1f} s)"}
     last = sts[-1]
     line = {"metric": TANDEM_METRIC, "value": value, "unit": TANDEM_UNIT, "n_gpus": world, "steps": args.steps,
@@ -500,7 +527,7 @@ def run_tandem(args, rank: int, world: int):
                     "d2h_bytes_per_step": int(last.d2h_bytes)},
             "gpu_launches": int(sum(s.launches for s in sts)),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                         "traffic": tandem_traffic(), "peak_source": "measured hbm_gbs" if peaks.get("hbm_gbs") else "fallback",
+                         "traffic": None, "peak_source": "measured hbm_gbs" if peaks.get("hbm_gbs") else "fallback",
                          "kernel": "k_tm_step", "algorithmic_bytes_per_track_step": TANDEM_BYTES["mixed"]},
             "roofline_l2": {"achieved": achieved, "peak": l2, "unit": "GB/s", "frac": achieved / l2 if l2 else None,
                             "peak_source": "L2 read bandwidth measured in this run (mq_measure_l2_read_gbs)"},
@@ -591,6 +618,8 @@ def main():
     clocks.start()
     dev_ms, step_ms, steps_total, launches, walls = [], [], 0, 0, []
     h2d = d2h = 0
+    moved, loads, replays, step_launches = 0.0, 0, 0, 0
+    wide = eng.tuning()["wide_records"]
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
@@ -606,6 +635,10 @@ def main():
         steps_total += s.ion_steps
         launches += s.kernel_launches
         h2d, d2h = s.h2d_bytes, s.d2h_bytes
+        moved += stepping_bytes(s, wide)
+        loads += s.cell_loads
+        replays += s.graph_replays
+        step_launches += s.step_kernel_launches
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
@@ -626,21 +659,20 @@ def main():
             s64 = e64.last_stats
         om = eng.run_batch(sj, dc, ph)
         sm = eng.last_stats
-        pulls = {}
-        for k in ("transmitted", "returned", "crashed", "timeout"):
-            a = int(getattr(om, k).sum())
-            b = int(getattr(o64, k).sum())
-            n = int(o64.n.sum())
-            p = (a + b + 1) / (2 * n + 2)
-            pulls[k] = {"mixed": a, "fp64": b, "pull": (a - b) / math.sqrt(2 * n * p * (1 - p))}
+        from multiq_workbench_gb300 import validate as V
+        cmp = V.compare_classes(V.class_counts(om), V.class_counts(o64))
         extra["fp64_gpu"] = {"value": s64.ion_steps / (s64.kernel_ms * 1e-3), "unit": UNIT,
                              "mixed_same_sample": sm.ion_steps / (sm.kernel_ms * 1e-3),
                              "speedup_mixed_over_fp64": (sm.ion_steps / sm.kernel_ms) / (s64.ion_steps / s64.kernel_ms),
-                             "sample": f"{sum(j.n for j in sj)} ions (16 of each job)", "outcomes": pulls}
+                             "fp64_note": "GB300's FP64 rate is a small fraction of its FP32 rate, which the ratio reflects",
+                             "sample": f"{sum(j.n for j in sj)} ions (16 of each job)",
+                             "outcomes": {"chi2": cmp["chi2"], "dof": cmp["dof"], "p": cmp["p"],
+                                          "classes": {k: {"mixed": c["a"], "fp64": c["b"], "pull": c["pull"]}
+                                                      for k, c in cmp["classes"].items()}}}
     cpu = None
     if rank == 0 and not args.no_cpu:
         r = cpu_rate(jobs, ph, dc, f, 128, os.cpu_count() or 1, target_s=12.0)
-        cpu = {"value": r["value"], "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+        cpu = {"value": r["value"], "unit": UNIT, "cores": os.cpu_count() or 1, "cpu": cpu_model(), "kind": "port",
                "sample": f"{r['ions']} ions of {r['jobs']} evenly spaced jobs run to completion ({r['seconds']:.1f} s)"}
 
     peaks = measured_peaks()
@@ -649,14 +681,7 @@ def main():
     l2 = l2_read_gbs(local) if rank == 0 else None
     hbm = hbm or 6800.0
     kern_s = sum(step_ms) * 1e-3
-    achieved = BYTES_PER_ION_STEP * steps_total / kern_s / 1e9
-    # DRAM bytes of one full-size k_mixed launch from the committed one-pass ncu summary
-    prof = ROOT / "profiles" / "k_mixed_batched_sweep_full.md"
-    traffic = None
-    if prof.exists():
-        import re
-        m = re.search(r"dram_bytes_per_launch:\s*([0-9.eE+]+)", prof.read_text())
-        traffic = float(m.group(1)) if m else None
+    achieved = moved / kern_s / 1e9
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
@@ -665,13 +690,19 @@ def main():
                                        f"({len(jobs) * args.ions_per_job:,} ions), "
                                        "0.100 mm channel grid 160x160x242, legacy half-kick, <=20000 steps",
                            "jobs": len(jobs), "ions": sum(j.n for j in jobs), "l2_flush": "256 MB write before every timed step",
-                           "tuning": tuned or eng.tuning()},
+                           "tuning": {**(tuned or eng.tuning()), "use_graph": replays > 0,
+                                      "graph_replays_per_step": replays / args.steps,
+                                      "step_launches_per_step": step_launches / args.steps}},
                 "ion_steps_per_step": steps_total / args.steps,
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
                 "gpu_launches": int(launches),
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                             "traffic": traffic, "peak_source": f"{peak_src} hbm_gbs",
-                             "kernel": "k_mixed", "algorithmic_bytes_per_ion_step": BYTES_PER_ION_STEP},
+                             "traffic": None, "peak_source": f"{peak_src} hbm_gbs",
+                             "kernel": "k_mixed",
+                             "algorithmic_bytes": f"cell fills counted by the kernel x 8 node records ({64 if wide else 48} B) "
+                                                  f"+ {ION_STATE_BYTES} B per ion taken from the queue",
+                             "algorithmic_bytes_per_ion_step": moved / max(steps_total, 1),
+                             "cell_loads_per_ion_step": loads / max(steps_total, 1)},
                 "roofline_l2": {"achieved": achieved, "peak": l2, "unit": "GB/s",
                                 "frac": achieved / l2 if l2 else None,
                                 "peak_source": "L2 read bandwidth measured in this run (mq_measure_l2_read_gbs: "

@@ -91,7 +91,11 @@ typedef struct mq_run_stats {
     uint64_t h2d_bytes, d2h_bytes;
     double step_kernel_ms;     /* device time of the stepping kernel(s) alone        */
     uint32_t step_kernel_launches;
-    uint32_t pad;
+    uint32_t graph_replays;    /* mixed engine: CUDA graph replays of its launch sequence     */
+    uint64_t cell_loads;       /* mixed engine: cell-cache fills of the stepping kernel, each
+                                  the 8 corner node records of one cell                     */
+    uint64_t ions_queued;      /* mixed engine: ions taken from the work queue, summed over the
+                                  launches (each reads and writes its working state once)   */
 } mq_run_stats;
 
 int32_t     mq_device_count(void);
@@ -181,14 +185,20 @@ mq_status   mq_check_selftest(int32_t device);
  *
  * Limits and rules:
  *  - njobs <= MQ_NOALLOC_MAX_JOBS; larger batches return MQ_ERR_TOO_LARGE (nothing is run).
+ *  - Jobs and physics are checked like every other entry point's (MQ_ERR_INVALID,
+ *    MQ_ERR_RF_MISMATCH), and every ion's jid must be < njobs: the call checks that on the
+ *    device first and returns MQ_ERR_INVALID, with the states untouched, if one is not.
  *  - The first call on a device looks up the scratch array's device address (once per
- *    device, with that device current); make that first call before any stream capture.
+ *    device and CUDA context, with that device current); make that first call before any
+ *    stream capture.
  *  - All calls share the one scratch array (its contents persist between calls; the call
  *    clears the counters it needs).  Calls that overlap on the GPU - from two host threads,
  *    or on two streams - race on it and must be serialised by the caller.
  *  - The drive phases are evaluated directly each step (the FP64 engine's phase tables are
  *    the same values, precomputed), so no table memory is needed.
- *  - Synchronous: returns after the last step, with *ion_steps (may be NULL) = executed steps.
+ *  - Synchronous: the call waits on `stream` (device-to-host reads of its counters after the
+ *    check and after every launch) and returns after the last step, with *ion_steps (may be
+ *    NULL) = executed steps.
  */
 #define MQ_NOALLOC_MAX_JOBS 4096
 #define MQ_NOALLOC_SCRATCH_BYTES (MQ_NOALLOC_MAX_JOBS * 96 + 256)

@@ -95,7 +95,8 @@ class mq_ions(C.Structure):
 class mq_run_stats(C.Structure):
     _fields_ = [("ion_steps", C.c_uint64), ("kernel_ms", C.c_double), ("launches", C.c_uint32),
                 ("kernel_launches", C.c_uint32), ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64),
-                ("step_kernel_ms", C.c_double), ("step_kernel_launches", C.c_uint32), ("pad", C.c_uint32)]
+                ("step_kernel_ms", C.c_double), ("step_kernel_launches", C.c_uint32), ("graph_replays", C.c_uint32),
+                ("cell_loads", C.c_uint64), ("ions_queued", C.c_uint64)]
 
 
 class mq_dev_grid(C.Structure):

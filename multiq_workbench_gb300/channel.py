@@ -284,11 +284,14 @@ class RunStats:
     d2h_bytes: int
     step_kernel_ms: float
     step_kernel_launches: int
+    graph_replays: int = 0     # mixed engine: CUDA graph replays of its launch sequence
+    cell_loads: int = 0        # mixed engine: cell-cache fills (8 corner node records each)
+    ions_queued: int = 0       # mixed engine: ions taken from the work queue over the launches
 
     @classmethod
     def from_native(cls, s: N.mq_run_stats) -> "RunStats":
         return cls(s.ion_steps, s.kernel_ms, s.launches, s.kernel_launches, s.h2d_bytes, s.d2h_bytes, s.step_kernel_ms,
-                   s.step_kernel_launches)
+                   s.step_kernel_launches, s.graph_replays, s.cell_loads, s.ions_queued)
 
 
 def device_count() -> int:

@@ -168,16 +168,9 @@ JobC make_job(const mq_job& j, const mq_physics& ph) {
 
 mq_status check_batch(mq_engine* e, const mq_job* jobs, size_t njobs, const mq_physics* ph) {
     if (!e) return MQ_ERR_INVALID;
-    if (!jobs || njobs == 0) return fail(e, MQ_ERR_INVALID, "a batch needs at least one job");   // channel.rs:444
-    if (!ph || !(ph->dt > 0) || !(ph->t_max >= 0) || !(ph->temp_k > 0) || !(ph->pressure_pa >= 0))
-        return fail(e, MQ_ERR_INVALID, "physics: dt, temp_k must be > 0 and t_max, pressure_pa >= 0");
-    for (size_t k = 0; k < njobs; ++k) {
-        if (jobs[k].drive.v_rf != jobs[0].drive.v_rf || jobs[k].drive.f_rf != jobs[0].drive.f_rf)
-            return fail(e, MQ_ERR_RF_MISMATCH, "RF drive must be shared by a batch");   // channel.rs:446
-        if (!(jobs[k].sp.mass > 0) || !(jobs[k].sp.z > 0) || !(jobs[k].sp.ccs_n2 >= 0))
-            return fail(e, MQ_ERR_INVALID, "species: mass and z must be > 0, ccs_n2 >= 0");
-    }
-    return MQ_OK;
+    const char* why = nullptr;
+    const mq_status s = mqd::check_jobs(jobs, njobs, ph, &why);
+    return s == MQ_OK ? MQ_OK : fail(e, s, why);
 }
 
 mqd::DevIons dev_ions(mq_engine* e) {
@@ -365,6 +358,9 @@ mq_status run_mixed(mq_engine* e, const mq_job* jobs, size_t njobs, const mq_phy
                                             " live ions");
     if (stats) {
         stats->launches += info.graph_replays;
+        stats->graph_replays += info.graph_replays;
+        stats->cell_loads += info.cell_loads;
+        stats->ions_queued += info.ions_queued;
         stats->kernel_launches += info.kernel_launches;
         stats->step_kernel_launches += info.step_launches;
         stats->step_kernel_ms += info.step_ms;
@@ -384,6 +380,26 @@ Batch host_batch(int32_t nx, int32_t ny, int32_t nz, double h, double axis_mm, c
     return make_batch(&tmp, ph, rf);
 }
 JobC host_job(const mq_job& j, const mq_physics& ph) { return make_job(j, ph); }
+
+mq_status check_jobs(const mq_job* jobs, size_t njobs, const mq_physics* ph, const char** why) {
+    *why = nullptr;
+    if (!jobs || njobs == 0) { *why = "a batch needs at least one job"; return MQ_ERR_INVALID; }   // channel.rs:444
+    if (!ph || !(ph->dt > 0) || !(ph->t_max >= 0) || !(ph->temp_k > 0) || !(ph->pressure_pa >= 0)) {
+        *why = "physics: dt, temp_k must be > 0 and t_max, pressure_pa >= 0";
+        return MQ_ERR_INVALID;
+    }
+    for (size_t k = 0; k < njobs; ++k) {
+        if (jobs[k].drive.v_rf != jobs[0].drive.v_rf || jobs[k].drive.f_rf != jobs[0].drive.f_rf) {
+            *why = "RF drive must be shared by a batch";   // channel.rs:446
+            return MQ_ERR_RF_MISMATCH;
+        }
+        if (!(jobs[k].sp.mass > 0) || !(jobs[k].sp.z > 0) || !(jobs[k].sp.ccs_n2 >= 0)) {
+            *why = "species: mass and z must be > 0, ccs_n2 >= 0";
+            return MQ_ERR_INVALID;
+        }
+    }
+    return MQ_OK;
+}
 }  // namespace mqd
 
 extern "C" {

@@ -54,5 +54,9 @@ namespace mqd {
 mqp::Batch host_batch(int32_t nx, int32_t ny, int32_t nz, double h, double axis_mm, const double layers_mm[8],
                       const mq_physics& ph, const mq_rfac& rf);
 mqp::JobC host_job(const mq_job& j, const mq_physics& ph);
+// the checks every batch entry point applies to its jobs and physics, without an engine: a batch
+// of at least one job sharing one RF drive, species with mass, z > 0 and ccs_n2 >= 0, physics with
+// dt, temp_k > 0 and t_max, pressure_pa >= 0.  Returns MQ_OK or the status, with *why the reason.
+int32_t check_jobs(const mq_job* jobs, size_t njobs, const mq_physics* ph, const char** why);
 
 }  // namespace mqd

@@ -32,12 +32,13 @@ using mqd::DevIons;
 
 constexpr unsigned FULL = 0xffffffffu;
 
-struct Ctrs {                       // device counters (32 B)
+struct Ctrs {                       // device counters (40 B)
     uint32_t head;                  // work-queue head of the current launch
     uint32_t count[2];              // live-list lengths (ping-pong)
     uint32_t pad;
     unsigned long long steps;       // executed ion-steps
-    unsigned long long pad2;
+    unsigned long long cell_loads;  // cell-cache fills (8 node records each)
+    unsigned long long queued;      // ions queued over the call's launches
 };
 
 // ---------------------------------------------------------------- Philox-4x32-10
@@ -186,6 +187,14 @@ __device__ __forceinline__ float field_comp(const float R[8], const float D[8], 
 
 __device__ __forceinline__ int32_t clampi(int32_t v, int32_t lo, int32_t hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
+// (xh + xl) - (th + tl) for a double-float position and threshold, as the sign-exact difference of
+// two double-floats: xh - th is exact wherever the two are within a factor of 2 of each other (which
+// covers every position close enough to the threshold for the low parts to matter), so the sign of
+// the result is the sign of the unrounded difference there
+__device__ __forceinline__ float df_diff(float xh, float xl, float th, float tl) {
+    return __fadd_rn(__fsub_rn(xh, th), __fsub_rn(xl, tl));
+}
+
 // ---------------------------------------------------------------- the persistent worker
 template <bool LEGACY, bool PREFETCH, bool WIDE>
 __global__ void __launch_bounds__(128, 3)
@@ -217,6 +226,7 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
     // 10-round generator runs with all lanes active instead of once per lane-boundary
     uint4 rc = make_uint4(0, 0, 0, 0), rn = make_uint4(0, 0, 0, 0);
     uint32_t iter = 0;
+    uint32_t loads = 0;                 // cell-cache fills of this lane
     Cell c;
     unsigned long long steps_total = 0;
 #pragma unroll
@@ -264,6 +274,7 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
                     if (!LEGACY) { rc = philox(k0, k1, n >> 2, 0u, 0u, 0u); rn = philox(k0, k1, (n >> 2) + 1u, 0u, 0u, 0u); }
                     load_cell<WIDE>(nodes, B, clampi(__float2int_rd(xh[0]), 0, B.nx - 2), clampi(__float2int_rd(xh[1]), 0, B.ny - 2),
                               clampi(__float2int_rd(xh[2]), 0, B.nz - 2), c);
+                    ++loads;
                     done = 0;
                     have = true;
                 } else {
@@ -390,7 +401,7 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
             if (ffi != c.fci || ffj != c.fcj || ffk != c.fck) {
                 const int32_t ci = clampi(__float2int_rd(xh[0]), 0, B.nx - 2), cj = clampi(__float2int_rd(xh[1]), 0, B.ny - 2),
                               ck = clampi(__float2int_rd(xh[2]), 0, B.nz - 2);
-                if (ci != c.ci || cj != c.cj || ck != c.ck) load_cell<WIDE>(nodes, B, ci, cj, ck, c);
+                if (ci != c.ci || cj != c.cj || ck != c.ck) { load_cell<WIDE>(nodes, B, ci, cj, ck, c); ++loads; }
             }
             if (PREFETCH) {
                 const int32_t pi = clampi(__float2int_rd(xh[0] + uh[0]), 0, B.nx - 2);
@@ -399,16 +410,17 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
                 if (pi != c.ci || pj != c.cj || pk != c.ck) prefetch_cell<WIDE>(nodes, B, pi, pj, pk);
             }
             // ---- termination tests: exit, return, box, conductor, timeout
-            // (a position exactly on a threshold is resolved by the high part alone; the box
-            // test is the unclamped cell index leaving [0, n-2])
+            // (the loss-surface planes - exit, return and the crash window - are crossed on the full
+            // double-float position against the double-float thresholds; the box test is the
+            // unclamped cell index leaving [0, n-2])
             int32_t status = 0;
-            if (xh[2] > B.z_exit_h) status = 3;
-            else if (xh[2] < B.z_ret_h) status = 2;
+            if (df_diff(xh[2], xl[2], B.z_exit_h, B.z_exit_l) > 0.0f) status = 3;
+            else if (df_diff(xh[2], xl[2], B.z_ret_h, B.z_ret_l) < 0.0f) status = 2;
             else if (ffi < 0.0f || ffj < 0.0f || ffk < 0.0f || ffi > B.lim_x - 1.0f || ffj > B.lim_y - 1.0f ||
                      ffk > B.lim_z - 1.0f)
                 status = 4;
             else {
-                if (xh[2] > B.cz0_h && xh[2] < B.cz1_h) {
+                if (df_diff(xh[2], xl[2], B.cz0_h, B.cz0_l) > 0.0f && df_diff(xh[2], xl[2], B.cz1_h, B.cz1_l) < 0.0f) {
                     const float fx = __fadd_rn(__fsub_rn(xh[0], c.fci), xl[0]);
                     const float fy = __fadd_rn(__fsub_rn(xh[1], c.fcj), xl[1]);
                     const float fz = __fadd_rn(__fsub_rn(xh[2], c.fck), xl[2]);
@@ -442,8 +454,12 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
         }
     }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) steps_total += __shfl_down_sync(FULL, steps_total, o);
+    for (int o = 16; o > 0; o >>= 1) {
+        steps_total += __shfl_down_sync(FULL, steps_total, o);
+        loads += __shfl_down_sync(FULL, loads, o);
+    }
     if (lane == 0 && steps_total) atomicAdd(&ctr->steps, steps_total);
+    if (lane == 0 && loads) atomicAdd(&ctr->cell_loads, (unsigned long long)loads);
 }
 
 // interleave RF | combined DC | AC into node records of `stride` float4 (once per DC configuration
@@ -608,10 +624,11 @@ __global__ void k_unstage(DevIons io, uint32_t n, MixBatch B, const float* __res
     }
 }
 
-// prepare launch: clear the queue head and the output count
+// prepare launch: clear the queue head and the output count, and add the launch's queue length
 __global__ void k_prep(Ctrs* ctr, int out_slot) {
     ctr->head = 0;
     ctr->count[out_slot] = 0;
+    ctr->queued += ctr->count[out_slot ^ 1];
 }
 
 void split(double v, float& h, float& l) {
@@ -855,6 +872,8 @@ cudaError_t run(Scratch& s, const Tuning& t, DevGrid g, uint64_t grid_gen, const
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
     cudaEventElapsedTime(&info->step_ms, s.ev[0], s.ev[1]);
     info->ion_steps = h.steps;
+    info->cell_loads = h.cell_loads;
+    info->ions_queued = h.queued;
     info->step_launches = launches;
     info->kernel_launches += kernels;
     // after the last launch the surviving list must be empty unless the step budget ran out

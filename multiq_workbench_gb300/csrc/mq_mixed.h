@@ -68,6 +68,8 @@ struct Scratch {
 
 struct RunInfo {
     uint64_t ion_steps = 0;
+    uint64_t cell_loads = 0;   // cell-cache fills of the stepping kernel (8 node records each)
+    uint64_t ions_queued = 0;  // ions taken from the work queue, summed over the launches
     float step_ms = 0.0f;
     uint32_t step_launches = 0;
     uint32_t kernel_launches = 0;

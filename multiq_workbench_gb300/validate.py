@@ -95,6 +95,90 @@ def table(title: str, a_name: str, b_name: str, a: Counts, b: Counts) -> str:
     return "\n".join(out)
 
 
+def _gamma_q(a: float, x: float) -> float:
+    """Regularised upper incomplete gamma Q(a, x): the power series of P below x = a + 1 and the
+    Lentz continued fraction of Q above (Press et al., Numerical Recipes, 3rd ed., section 6.2)."""
+    if x <= 0.0:
+        return 1.0
+    lg = math.lgamma(a)
+    if x < a + 1.0:
+        term = total = 1.0 / a
+        ap = a
+        for _ in range(10_000):
+            ap += 1.0
+            term *= x / ap
+            total += term
+            if abs(term) < abs(total) * 1e-15:
+                break
+        return max(0.0, 1.0 - total * math.exp(-x + a * math.log(x) - lg))
+    tiny = 1e-300
+    b = x + 1.0 - a
+    c = 1.0 / tiny
+    d = 1.0 / b
+    h = d
+    for i in range(1, 10_000):
+        an = -i * (i - a)
+        b += 2.0
+        d = an * d + b
+        d = tiny if abs(d) < tiny else d
+        c = b + an / c
+        c = tiny if abs(c) < tiny else c
+        d = 1.0 / d
+        delta = d * c
+        h *= delta
+        if abs(delta - 1.0) < 1e-15:
+            break
+    return math.exp(-x + a * math.log(x) - lg) * h
+
+
+def chi2_sf(x: float, dof: int) -> float:
+    """P(X >= x) for X chi-square distributed with ``dof`` degrees of freedom (1 when dof = 0)."""
+    return 1.0 if dof <= 0 else _gamma_q(0.5 * dof, 0.5 * x)
+
+
+def compare_classes(a: dict, b: dict) -> dict:
+    """Outcome-class counts of two engines run on the same ions with independent random streams
+    (``a`` and ``b``: class name -> count, each summing to the same n): the chi-square test of
+    homogeneity of the 2 x K table of classes with a non-zero total (K - 1 degrees of freedom),
+    its p-value, and per class the pooled binomial pull of the two fractions, (a / na - b / nb) /
+    sqrt(p (1 - p) (1 / na + 1 / nb)) with p the pooled fraction."""
+    keys = [k for k in a if a[k] + b[k] > 0]
+    na, nb = sum(a.values()), sum(b.values())
+    tot = na + nb
+    stat = 0.0
+    pulls = {}
+    for k in keys:
+        col = a[k] + b[k]
+        for obs, rowsum in ((a[k], na), (b[k], nb)):
+            e = rowsum * col / tot
+            stat += (obs - e) ** 2 / e
+        p = col / tot
+        se = math.sqrt(p * (1 - p) * (1.0 / na + 1.0 / nb)) if 0 < p < 1 else 0.0
+        pulls[k] = {"a": int(a[k]), "b": int(b[k]), "pull": (a[k] / na - b[k] / nb) / se if se > 0 else 0.0}
+    dof = max(len(keys) - 1, 0)
+    return {"chi2": stat, "dof": dof, "p": chi2_sf(stat, dof), "n": [int(na), int(nb)], "classes": pulls}
+
+
+def compare_jobs(a_jobs: list, b_jobs: list) -> dict:
+    """Per-job homogeneity over many jobs: the sum of each job's 2 x K chi-square and of its degrees
+    of freedom (the jobs are independent), with the p-value of the sum."""
+    stat, dof = 0.0, 0
+    for a, b in zip(a_jobs, b_jobs):
+        r = compare_classes(a, b)
+        stat += r["chi2"]
+        dof += r["dof"]
+    return {"chi2": stat, "dof": dof, "p": chi2_sf(stat, dof), "jobs": len(a_jobs)}
+
+
+CLASSES = ("crashed", "returned", "transmitted", "left", "timeout")
+
+
+def class_counts(outs, jobs=None) -> dict:
+    """Outcome-class totals of a batch's ``Outcomes`` (all jobs, or the job indices in ``jobs``)."""
+    idx = range(len(outs)) if jobs is None else jobs
+    return {k: int(sum(getattr(outs[j], k) for j in idx)) for k in CLASSES}
+
+
 def s14_fields(device: int | None = 0) -> Fields:
     """The calibrated S14 channel ("code" variant, hole 7.0 mm; validate.rs:98)."""
     return Fields.build(Geom.s14("code", hole_d=7.0), device=device)

@@ -117,3 +117,33 @@ def test_l2_probe_refusals_without_device(built):
 def test_fault_injection_needs_an_engine(built):
     from multiq_workbench_gb300 import _native as N
     assert N.lib().mq_engine_inject_fault(None, 1) == -1
+
+
+def test_noalloc_entry_refuses_bad_jobs_and_physics(built):
+    """The allocation-free entry point applies the job and physics checks of every other entry
+    point before it touches a device: zero mass, zero charge, negative CCS, zero temperature,
+    negative pressure or t_max, and a batch whose RF drives differ are refused (the pointers are
+    never dereferenced: the checks come first)."""
+    import dataclasses
+    import multiq_workbench_gb300 as mq
+    from multiq_workbench_gb300 import _native as N
+    from multiq_workbench_gb300.channel import jobs_native
+    grid = N.mq_dev_grid()
+    grid.nx = grid.ny = grid.nz = 8
+    grid.h = 1e-3
+    grid.rf4 = grid.ac4 = grid.dc4 = 1
+    io = N.mq_ions()
+    for k, _ in mq.channel.ION_FIELDS:
+        setattr(io, k, 1)
+    good = mq.Physics(pressure_pa=0.1)
+    drive = mq.RfAc(100.0, 500e3, 0.5, 1e5)
+
+    def call(jobs, ph):
+        return N.lib().mq_run_ions_device_noalloc(C.byref(grid), jobs_native(jobs), len(jobs), C.byref(ph.native()),
+                                                  C.byref(io), 4, 10, None, None)
+    for sp in (mq.Species(0.0, 1.0, 185.6), mq.Species(499.0, 0.0, 185.6), mq.Species(499.0, 1.0, -1.0)):
+        assert call([mq.Job(sp, drive, 4, 1)], good) == -1, sp
+    sp = mq.Species(499.0, 1.0, 185.6)
+    for bad in (dict(temp_k=0.0), dict(pressure_pa=-1.0), dict(t_max=-1e-6), dict(dt=0.0)):
+        assert call([mq.Job(sp, drive, 4, 1)], dataclasses.replace(good, **bad)) == -1, bad
+    assert call([mq.Job(sp, drive, 2, 1), mq.Job(sp, mq.RfAc(90.0, 500e3, 0.5, 1e5), 2, 2)], good) == -5

@@ -26,3 +26,28 @@ def test_embedded_reference_counts_and_point():
     ph = V.point_physics(True)
     assert ph.t_max == 3e-3 and ph.pressure_pa == 0.1 and ph.rf_phase0
     assert not V.point_physics(False).rf_phase0
+
+
+def test_chi2_survival_matches_scipy():
+    stats = __import__("pytest").importorskip("scipy.stats")
+    for dof in (1, 2, 3, 4, 7, 24, 36, 100):
+        for x in (0.01, 0.5, 1.0, 3.0, 7.5, 20.0, 40.0, 80.0, 150.0):
+            assert math.isclose(V.chi2_sf(x, dof), stats.chi2.sf(x, dof), rel_tol=1e-9, abs_tol=1e-12), (dof, x)
+    assert V.chi2_sf(3.0, 0) == 1.0
+
+
+def test_class_comparison_is_the_contingency_chi2():
+    stats = __import__("pytest").importorskip("scipy.stats")
+    a = {"crashed": 400, "returned": 300, "transmitted": 250, "left": 50, "timeout": 0}
+    b = {"crashed": 420, "returned": 280, "transmitted": 240, "left": 60, "timeout": 0}
+    r = V.compare_classes(a, b)
+    c = stats.chi2_contingency([[400, 300, 250, 50], [420, 280, 240, 60]], correction=False)
+    assert math.isclose(r["chi2"], c[0], rel_tol=1e-12) and r["dof"] == 3 and math.isclose(r["p"], c[1], rel_tol=1e-9)
+    p = 820 / 2000
+    assert math.isclose(r["classes"]["crashed"]["pull"], (0.4 - 0.42) / math.sqrt(p * (1 - p) * 2 / 1000))
+    assert "timeout" not in r["classes"]
+    # identical tables: chi2 0, p 1; one class only: no degrees of freedom
+    assert V.compare_classes(a, a)["p"] == 1.0
+    assert V.compare_classes({"crashed": 5}, {"crashed": 5})["dof"] == 0
+    j = V.compare_jobs([a, a], [b, a])
+    assert math.isclose(j["chi2"], r["chi2"]) and j["dof"] == 6

@@ -86,6 +86,42 @@ def test_noalloc_matches_fp64_entry_point_on_two_calls(setup):
     assert (got2.status != 0).all()
 
 
+def test_noalloc_refuses_an_ion_whose_job_index_is_out_of_range(setup):
+    """The states are device memory, so the call checks every ion's job index on the device before
+    stepping: one index equal to njobs makes it return MQ_ERR_INVALID with the states untouched,
+    and the next call with good indices runs as before."""
+    import torch
+    mq, f, dc, ph, jobs = setup
+    from multiq_workbench_gb300 import _native as N
+    from multiq_workbench_gb300.channel import jobs_native
+    start = mq.inject(f, jobs, ph)
+    bad = start.copy()
+    bad.jid[17] = len(jobs)
+    dev = {k: torch.from_numpy(np.ascontiguousarray(getattr(bad, k))).cuda() for k in FIELDS}
+    rf, ac, dcf = (torch.from_numpy(a).cuda() for a in (f.rf, f.ac, f.dc_field(dc)))
+    grid = N.mq_dev_grid()
+    grid.nx, grid.ny, grid.nz, grid.h = f.nx, f.ny, f.nz, f.h
+    grid.rf4, grid.ac4, grid.dc4 = rf.data_ptr(), ac.data_ptr(), dcf.data_ptr()
+    grid.axis_mm = f.geom.axis()
+    for i, v in enumerate(f.geom.layers()):
+        grid.layers_mm[i] = v
+    io = N.mq_ions()
+    for k in FIELDS:
+        setattr(io, k, dev[k].data_ptr())
+    torch.cuda.synchronize()
+    code = N.lib().mq_run_ions_device_noalloc(C.byref(grid), jobs_native(jobs), len(jobs), C.byref(ph.native()),
+                                              C.byref(io), len(start), 100, None, None)
+    assert code == -1     # MQ_ERR_INVALID
+    for k in FIELDS:
+        assert np.array_equal(dev[k].cpu().numpy().view(np.uint8), getattr(bad, k).view(np.uint8)), k
+    got, _ = _device_call(mq, f, dc, ph, jobs, start, 100)
+    ref = start.copy()
+    with mq.Engine(f, mq.PREC_F64) as e:
+        e.set_dc(dc)
+        e.run_ions(jobs, ph, ref, max_more=100)
+    _same(got, ref, "after a refused call")
+
+
 def test_noalloc_rejects_batches_beyond_its_scratch(setup):
     mq, f, dc, ph, jobs = setup
     from multiq_workbench_gb300 import _native as N
