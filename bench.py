@@ -207,6 +207,113 @@ def run_gridstudy(args, rank: int, world: int):
     print(json.dumps(line), flush=True)
 
 
+LEGACY_METRIC = "ion-steps/s, 1 GB300: legacy Fig. 4 mass scan (legacy collisions), mixed precision vs plain FP64"
+
+
+def legacy_workload(replicas: int = 40):
+    """The reference's legacy Fig. 4 scan (chsim legacy-fig4): m/z 475..525 step 2 (26 values) of 5+
+    ions (mass 5 m/z), 100 V / 500 kHz RF, 0.5 V / 100 kHz excitation, DC [0, +5, -5, 0] V, every
+    legacy switch (half kick, stationary-gas collisions every mean free path, nearest-node fields,
+    point-and-cone launch, legacy criteria), 1 mTorr; 1,000 ions per m/z, replicated over ``replicas``
+    seed sets to fill the GPU (26,000 x replicas ions)."""
+    import multiq_workbench_gb300 as mq
+    from multiq_workbench_gb300 import chsim as CH
+    mzs = [475.0 + 2.0 * i for i in range(26)]
+    jobs = [mq.Job(mq.Species(mz * 5.0, 5.0, 0.0), CH.FIG4_DRIVE, 1000, 1000 * r + int(mz))
+            for r in range(replicas) for mz in mzs]
+    return jobs, mq.Physics.legacy(1e-3 * 133.322), list(CH.FIG4_DC)
+
+
+def run_legacy(args, rank: int, world: int):
+    """The legacy-collision path: the Fig. 4 scan x 40 seed sets (1,040,000 ions) on the 0.100 mm grid,
+    the mixed engine timed (``k_mixed`` with legacy collisions), the FP64 kernel on one seed set
+    (26,000 ions) for the speed ratio and the class counts, and the CPU oracle on a sample."""
+    import torch
+    import __graft_entry__ as ge
+    import multiq_workbench_gb300 as mq
+    from multiq_workbench_gb300 import validate as V
+    ge.build()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    jobs, ph, dc = legacy_workload()
+    if rank:
+        jobs = [mq.Job(j.sp, j.drive, j.n, j.seed + rank_seed0(rank)) for j in jobs]
+    f = mq.Fields.build(mq.Geom(), bases=[0, 1, 3, 4], cache=False, device=local)
+    table = mq.JobTable.from_jobs(jobs, pinned=True)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+    eng = mq.Engine(f, mq.PREC_MIXED, device=local)
+    tuned = eng.tuning()
+    for _ in range(args.warmup):
+        eng.run_batch(table, dc, ph)
+    clocks = Clocks(local)
+    clocks.start()
+    ms, step_ms, walls, steps, moved, loads, launches = [], [], [], 0, 0.0, 0, 0
+    for _ in range(args.steps):
+        flush_l2(flush)
+        torch.cuda.synchronize()
+        w0 = time.perf_counter()
+        out = eng.run_batch(table, dc, ph)
+        walls.append(time.perf_counter() - w0)
+        st = eng.last_stats
+        ms.append(st.kernel_ms)
+        step_ms.append(st.step_kernel_ms)
+        steps += st.ion_steps
+        moved += stepping_bytes(st, tuned["wide_records"])
+        loads += st.cell_loads
+        launches += st.kernel_launches
+        h2d, d2h = st.h2d_bytes, st.d2h_bytes
+    clk = clocks.stop()
+    (t_dev, t_wall), (steps_all,) = reduce_over_ranks([sum(ms) * 1e-3, sum(walls)], [steps], f"cuda:{local}")
+    if rank != 0:
+        eng.close()
+        return
+    sample = jobs[:26]
+    om = eng.run_batch(sample, dc, ph)
+    sm = eng.last_stats
+    eng.close()
+    extra = {}
+    if not args.no_f64:
+        with mq.Engine(f, mq.PREC_F64, device=local) as e64:
+            o64 = e64.run_batch(sample, dc, ph)
+            s64 = e64.last_stats
+        cmp = V.compare_classes(V.class_counts(om), V.class_counts(o64))
+        extra["fp64_gpu"] = {"value": s64.ion_steps / (s64.kernel_ms * 1e-3), "unit": UNIT,
+                             "mixed_same_sample": sm.ion_steps / (sm.kernel_ms * 1e-3),
+                             "speedup_mixed_over_fp64": (sm.ion_steps / sm.kernel_ms) / (s64.ion_steps / s64.kernel_ms),
+                             "sample": "one seed set: 26 m/z x 1,000 ions",
+                             "outcomes": {"chi2": cmp["chi2"], "dof": cmp["dof"], "p": cmp["p"],
+                                          "classes": {k: {"mixed": c["a"], "fp64": c["b"], "pull": c["pull"]}
+                                                      for k, c in cmp["classes"].items()}}}
+    cpu = None
+    if not args.no_cpu:
+        r = cpu_rate(jobs, ph, dc, f, 26, os.cpu_count() or 1, target_s=12.0)
+        cpu = {"value": r["value"], "unit": UNIT, "cores": os.cpu_count() or 1, "cpu": cpu_model(), "kind": "port",
+               "sample": f"{r['ions']} ions of {r['jobs']} evenly spaced jobs run to completion ({r['seconds']:.1f} s)"}
+    peaks = measured_peaks()
+    hbm = peaks.get("hbm_gbs") or 6800.0
+    l2 = l2_read_gbs(local)
+    kern_s = sum(step_ms) * 1e-3
+    achieved = moved / kern_s / 1e9
+    line = {"metric": LEGACY_METRIC, "value": steps_all / t_dev, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+            "config": {"workload": f"legacy Fig. 4 scan: 26 m/z (475-525) x 1,000 ions x 40 seed sets "
+                                   f"({table.total_ions():,} ions), Physics::legacy(1 mTorr), 0.100 mm grid",
+                       "l2_flush": "256 MB write before every timed step", "tuning": tuned},
+            "ion_steps_per_step": steps / args.steps,
+            "e2e": {"value": steps_all / t_wall, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+            "gpu_launches": int(launches),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                         "traffic": None, "peak_source": "measured hbm_gbs" if peaks.get("hbm_gbs") else "fallback",
+                         "kernel": "k_mixed (legacy collisions)",
+                         "cell_loads_per_ion_step": loads / max(steps, 1)},
+            "roofline_l2": {"achieved": achieved, "peak": l2, "unit": "GB/s", "frac": achieved / l2 if l2 else None},
+            "cpu_baseline": cpu, "clocks": clk,
+            "outcomes": {k: int(getattr(out, k).sum()) for k in V.CLASSES}}
+    line.update(extra)
+    print(json.dumps(line), flush=True)
+
+
 class Clocks:
     """nvidia-smi sampling during the timed region."""
 
@@ -554,9 +661,10 @@ def main():
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--ions-per-job", type=int, default=256,
                     help="ions per job (256 = the benchmark workload; smaller = a profiling case)")
-    ap.add_argument("--workload", default="sweep", choices=["sweep", "tandem", "gridstudy"],
+    ap.add_argument("--workload", default="sweep", choices=["sweep", "tandem", "gridstudy", "legacy"],
                     help="sweep: the batched channel sweep (default); tandem: the nine-channel tandem transport; "
-                         "gridstudy: one launch on grids solved at 0.100 / 0.050 / 0.0333 mm")
+                         "gridstudy: one launch on grids solved at 0.100 / 0.050 / 0.0333 mm; legacy: the Fig. 4 "
+                         "mass scan with every legacy switch (legacy collisions)")
     ap.add_argument("--tracks", type=int, default=1 << 20, help="tandem: tracks in the pulse")
     ap.add_argument("--tandem-steps", type=int, default=1000, help="tandem: global steps per bench step")
     ap.add_argument("--port-h", type=float, default=0.05, help="tandem: port grid spacing [mm]")
@@ -579,6 +687,18 @@ def main():
                                                  "--impl reference without --workload for it"}), flush=True)
         else:
             run_gridstudy(args, rank, world)
+        if dist:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+    if args.workload == "legacy":
+        if args.impl == "reference":
+            if rank == 0:
+                print(json.dumps({"impl": "reference", "metric": LEGACY_METRIC,
+                                  "unavailable": "the legacy scan's reference arm is the sweep's CPU port; run "
+                                                 "--impl reference without --workload for it"}), flush=True)
+        else:
+            run_legacy(args, rank, world)
         if dist:
             dist.barrier()
             dist.destroy_process_group()

@@ -124,6 +124,9 @@ mq_status   mq_run_ions(mq_engine* e, const mq_job* jobs, size_t njobs, const mq
 mq_status   mq_run_batch(mq_engine* e, const mq_job* jobs, size_t njobs, const double dc[4], const mq_physics* ph,
                          mq_outcome* out, mq_ions* ions_out, mq_run_stats* stats);
 mq_status   mq_summarize(const mq_ions* io, size_t n, double dt, size_t njobs, mq_outcome* out);
+/* FNV-1a 64 of `bytes` bytes, continuing from hash `h` (start with 1469598103934665603): the hash
+ * chsim's self-check prints over final ion states (fnv, simulation/chsim/src/check.rs:95-99). */
+uint64_t    mq_fnv1a64(const void* data, size_t bytes, uint64_t h);
 
 /* Launch shape of the mixed engine (no counterpart in the reference, whose worker shape is
  * fixed by #defines and environment variables: simulation/chsim/src/tiled.rs:10-29). */
@@ -135,6 +138,8 @@ typedef struct mq_tuning {
     int32_t prefetch;            /* L1-prefetch the cell each ion is heading for           */
     int32_t wide_records;        /* 64-byte node records read with 256-bit loads (else 48 B;
                                     needs 4 x nodes below 2^32)                            */
+    int32_t sort_cells;          /* before every launch, put the live ions in the Morton order
+                                    of their cells (a counting sort on the device)         */
 } mq_tuning;
 mq_status   mq_engine_get_tuning(mq_engine* e, mq_tuning* t);
 mq_status   mq_engine_set_tuning(mq_engine* e, const mq_tuning* t);

@@ -108,7 +108,7 @@ class mq_dev_grid(C.Structure):
 class mq_tuning(C.Structure):
     _fields_ = [("threads_per_block", C.c_int32), ("blocks_per_sm", C.c_int32), ("chunk", C.c_uint32),
                 ("use_graph", C.c_int32), ("prefetch", C.c_int32),
-                ("wide_records", C.c_int32)]
+                ("wide_records", C.c_int32), ("sort_cells", C.c_int32)]
 
 
 class mq_cube_geom(C.Structure):
@@ -317,6 +317,8 @@ def _declare_engine(L) -> None:
     L.mq_run_batch.restype = C.c_int32
     L.mq_summarize.argtypes = [P(mq_ions), C.c_size_t, C.c_double, C.c_size_t, P(mq_outcome)]
     L.mq_summarize.restype = C.c_int32
+    L.mq_fnv1a64.argtypes = [C.c_void_p, C.c_size_t, C.c_uint64]
+    L.mq_fnv1a64.restype = C.c_uint64
     L.mq_device_count.argtypes = []
     L.mq_device_count.restype = C.c_int32
     L.mq_measure_l2_read_gbs.argtypes = [C.c_int32, C.c_size_t, C.c_int32, P(C.c_double)]

@@ -331,18 +331,21 @@ class Engine:
         t = N.mq_tuning()
         N.check(N.lib().mq_engine_get_tuning(self._h, C.byref(t)), "mq_engine_get_tuning", self._h)
         return dict(threads_per_block=t.threads_per_block, blocks_per_sm=t.blocks_per_sm, chunk=t.chunk,
-                    use_graph=bool(t.use_graph), prefetch=bool(t.prefetch), wide_records=bool(t.wide_records))
+                    use_graph=bool(t.use_graph), prefetch=bool(t.prefetch), wide_records=bool(t.wide_records),
+                    sort_cells=bool(t.sort_cells))
 
     def set_tuning(self, blocks_per_sm: int | None = None, chunk: int | None = None, use_graph: bool | None = None,
-                   prefetch: bool | None = None, wide_records: bool | None = None) -> None:
+                   prefetch: bool | None = None, wide_records: bool | None = None, sort_cells: bool | None = None) -> None:
         """Override the mixed engine's launch shape; ``wide_records`` picks 64-byte node records read
-        with 256-bit loads (the default on grids below 1 GB of 48-byte records) over 48-byte ones."""
+        with 256-bit loads (the default on grids below 1 GB of 48-byte records) over 48-byte ones;
+        ``sort_cells`` puts every launch's live ions in the Morton order of their cells."""
         cur = self.tuning()
         t = N.mq_tuning(128, int(blocks_per_sm if blocks_per_sm is not None else cur["blocks_per_sm"]),
                         int(chunk if chunk is not None else cur["chunk"]),
                         int(use_graph if use_graph is not None else cur["use_graph"]),
                         int(prefetch if prefetch is not None else cur["prefetch"]),
-                        int(wide_records if wide_records is not None else cur["wide_records"]))
+                        int(wide_records if wide_records is not None else cur["wide_records"]),
+                        int(sort_cells if sort_cells is not None else cur["sort_cells"]))
         N.check(N.lib().mq_engine_set_tuning(self._h, C.byref(t)), "mq_engine_set_tuning", self._h)
 
     def autotune(self, jobs, dc, ph: Physics, sample_per_job: int = 2048) -> tuple[dict, float]:

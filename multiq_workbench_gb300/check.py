@@ -43,10 +43,11 @@ def check_case(engine, jobs, dc, ph) -> dict:
 
 
 def hash_ions(ions: IonStates) -> int:
-    """FNV-1a 64 over every ion's final state, field by field in ``ION_FIELDS`` order (check.rs:92-96)."""
+    """FNV-1a 64 over every ion's final state, field by field in ``ION_FIELDS`` order (check.rs:95-99),
+    computed by the native library (``mq_fnv1a64``)."""
+    from . import _native as N
     h = 1469598103934665603
-    data = b"".join(np.ascontiguousarray(getattr(ions, name)).tobytes() for name, _ in ION_FIELDS)
-    for b in data:
-        h ^= b
-        h = (h * 1099511628211) & 0xFFFFFFFFFFFFFFFF
+    for name, _ in ION_FIELDS:
+        a = np.ascontiguousarray(getattr(ions, name))
+        h = int(N.lib().mq_fnv1a64(a.ctypes.data, a.nbytes, h))
     return h

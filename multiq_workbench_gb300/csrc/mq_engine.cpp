@@ -621,6 +621,7 @@ mq_status mq_engine_get_tuning(mq_engine* e, mq_tuning* t) {
     t->use_graph = e->tune.use_graph;
     t->prefetch = e->tune.prefetch;
     t->wide_records = e->tune.wide;
+    t->sort_cells = e->tune.sort_cells;
     return MQ_OK;
 }
 
@@ -636,6 +637,7 @@ mq_status mq_engine_set_tuning(mq_engine* e, const mq_tuning* t) {
     e->tune.use_graph = t->use_graph ? 1 : 0;
     e->tune.prefetch = t->prefetch ? 1 : 0;
     e->tune.wide = t->wide_records ? 1 : 0;
+    e->tune.sort_cells = t->sort_cells ? 1 : 0;
     return MQ_OK;
 }
 
@@ -726,6 +728,15 @@ mq_status mq_engine_autotune(mq_engine* e, const mq_job* jobs, size_t njobs, con
     if (best) mq_engine_get_tuning(e, best);
     if (best_rate) *best_rate = top_rate;
     return MQ_OK;
+}
+
+uint64_t mq_fnv1a64(const void* data, size_t bytes, uint64_t h) {
+    const unsigned char* p = static_cast<const unsigned char*>(data);
+    for (size_t i = 0; i < bytes; ++i) {
+        h ^= (uint64_t)p[i];
+        h *= 1099511628211ull;
+    }
+    return h;
 }
 
 mq_status mq_summarize(const mq_ions* io, size_t n, double dt, size_t njobs, mq_outcome* out) {

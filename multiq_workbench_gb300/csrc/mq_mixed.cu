@@ -624,6 +624,92 @@ __global__ void k_unstage(DevIons io, uint32_t n, MixBatch B, const float* __res
     }
 }
 
+// ---------------------------------------------------------------- cell order of the live list
+// Before a launch, the live list can be put in the Morton order of the ions' cells (a counting sort
+// on the top bits of the 30-bit code), so the 32 lanes of a warp, which take consecutive queue
+// slots, start in neighbouring cells and share cache lines in their cell gathers.  Order within a
+// bin is the atomics' arrival order: per-ion results do not depend on the order.
+// Bits 0..9 of v spread to every third bit (the "part 1 by 2" step of Morton encoding).
+__device__ __forceinline__ uint32_t spread10(uint32_t v) {
+    v &= 0x3ffu;
+    v = (v ^ (v << 16)) & 0xff0000ffu;
+    v = (v ^ (v << 8)) & 0x0300f00fu;
+    v = (v ^ (v << 4)) & 0x030c30c3u;
+    v = (v ^ (v << 2)) & 0x09249249u;
+    return v;
+}
+
+constexpr int kScanBlock = 1024;          // threads of the scan kernels
+constexpr int kScanItems = 4;             // bins per scan thread
+constexpr uint32_t kScanTile = kScanBlock * kScanItems;
+
+// bin of every listed ion (cell Morton code >> shift) and the bins' counts
+__global__ void k_sort_keys(const uint32_t* __restrict__ list, const Ctrs* __restrict__ ctr, int slot,
+                            const float* __restrict__ keep, uint32_t n_all, MixBatch B, uint32_t shift,
+                            uint32_t* __restrict__ keys, uint32_t* __restrict__ bins) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ctr->count[slot]) return;
+    const uint32_t id = list[t];
+    const uint32_t ci = (uint32_t)clampi(__float2int_rd(keep[(size_t)0 * n_all + id]), 0, B.nx - 2);
+    const uint32_t cj = (uint32_t)clampi(__float2int_rd(keep[(size_t)1 * n_all + id]), 0, B.ny - 2);
+    const uint32_t ck = (uint32_t)clampi(__float2int_rd(keep[(size_t)2 * n_all + id]), 0, B.nz - 2);
+    const uint32_t key = (spread10(ci) | (spread10(cj) << 1) | (spread10(ck) << 2)) >> shift;
+    keys[t] = key;
+    atomicAdd(bins + key, 1u);
+}
+
+// exclusive scan of a tile of kScanTile counts in place; the tile's total to sums[blockIdx.x]
+__global__ void __launch_bounds__(kScanBlock) k_scan_tiles(uint32_t* __restrict__ v, uint32_t n, uint32_t* __restrict__ sums) {
+    __shared__ uint32_t warp_tot[kScanBlock / 32];
+    const uint32_t base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    uint32_t x[kScanItems], run = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        x[k] = base + k < n ? v[base + k] : 0u;
+        run += x[k];
+    }
+    const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint32_t inc = run;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(FULL, inc, o);
+        if (lane >= (uint32_t)o) inc += y;
+    }
+    if (lane == 31) warp_tot[w] = inc;
+    __syncthreads();
+    if (w == 0) {
+        uint32_t t = warp_tot[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(FULL, t, o);
+            if (lane >= (uint32_t)o) t += y;
+        }
+        warp_tot[lane] = t;   // inclusive over warps
+    }
+    __syncthreads();
+    uint32_t off = inc - run + (w ? warp_tot[w - 1] : 0u);
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        if (base + k < n) v[base + k] = off;
+        off += x[k];
+    }
+    if (threadIdx.x == kScanBlock - 1) sums[blockIdx.x] = warp_tot[kScanBlock / 32 - 1];
+}
+
+// add the scanned tile totals to every tile
+__global__ void k_scan_add(uint32_t* __restrict__ v, uint32_t n, const uint32_t* __restrict__ sums) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) v[i] += sums[i / kScanTile];
+}
+
+// every listed ion to the next free place of its bin
+__global__ void k_sort_scatter(const uint32_t* __restrict__ list, const Ctrs* __restrict__ ctr, int slot,
+                               const uint32_t* __restrict__ keys, uint32_t* __restrict__ bins, uint32_t* __restrict__ out) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ctr->count[slot]) return;
+    out[atomicAdd(bins + keys[t], 1u)] = list[t];
+}
+
 // prepare launch: clear the queue head and the output count, and add the launch's queue length
 __global__ void k_prep(Ctrs* ctr, int out_slot) {
     ctr->head = 0;
@@ -726,9 +812,32 @@ Tuning default_tuning(int device, size_t nodes) {
 
 void release(Scratch& s) {
     if (s.graph) cudaGraphExecDestroy(s.graph);
-    for (void* p : {s.lists, s.ctrs, s.params, s.jobs, s.nodes, s.keep}) if (p) cudaFree(p);
+    for (void* p : {s.lists, s.ctrs, s.params, s.jobs, s.nodes, s.keep, s.sort}) if (p) cudaFree(p);
     for (auto& e : s.ev) if (e) cudaEventDestroy(e);
     s = Scratch();
+}
+
+// bins of the cell sort: the top min(22, 3 b) bits of the Morton code, b the bits of the largest
+// cell index (nbins <= 2^22, so the tile totals fit one scan tile)
+struct SortPlan {
+    uint32_t nbins, tiles, shift;
+};
+static SortPlan sort_plan(const MixBatch& mb, uint32_t n) {
+    (void)n;
+    int32_t mx = mb.nx > mb.ny ? mb.nx : mb.ny;
+    mx = mx > mb.nz ? mx : mb.nz;
+    uint32_t bits = 1;
+    while ((1u << bits) < (uint32_t)(mx - 1)) ++bits;   // cell indices 0 .. mx - 2
+    const uint32_t code = 3 * bits, kb = code < 22 ? code : 22;
+    SortPlan p;
+    p.nbins = 1u << kb;
+    p.tiles = (p.nbins + kScanTile - 1) / kScanTile;
+    p.shift = code - kb;
+    return p;
+}
+static size_t sort_bytes(const MixBatch& mb, uint32_t n) {
+    const SortPlan p = sort_plan(mb, n);
+    return sizeof(uint32_t) * ((size_t)p.nbins + p.tiles + 1 + 2 * (size_t)n);
 }
 
 static cudaError_t enqueue_launches(const Scratch& s, const Tuning& t, const MixBatch& mb, DevIons io,
@@ -741,12 +850,28 @@ static cudaError_t enqueue_launches(const Scratch& s, const Tuning& t, const Mix
     uint64_t* kph = static_cast<uint64_t*>(s.keep);
     float* keep = reinterpret_cast<float*>(kph + (size_t)2 * n);
     const int grid = t.sms * t.blocks_per_sm;
+    const SortPlan sp = sort_plan(mb, n);
+    uint32_t* bins = static_cast<uint32_t*>(s.sort);
+    uint32_t* sums = bins + sp.nbins;
+    uint32_t* keys = sums + sp.tiles + 1;
+    uint32_t* sorted = keys + n;
     for (uint32_t L = 0; L < launches; ++L) {
         const int in = (int)(L & 1);
         k_prep<<<1, 1, 0, st>>>(ctr, in ^ 1);
         const uint32_t ch = (L + 1 == launches) ? last_chunk : chunk;
         const uint32_t* li = lists + (size_t)in * n;
         uint32_t* lo = lists + (size_t)(in ^ 1) * n;
+        if (t.sort_cells) {   // this launch's list in the cells' Morton order
+            cudaMemsetAsync(bins, 0, (size_t)sp.nbins * sizeof(uint32_t), st);
+            const unsigned gi = (n + 255) / 256;
+            k_sort_keys<<<gi, 256, 0, st>>>(li, ctr, in, keep, n, mb, sp.shift, keys, bins);
+            k_scan_tiles<<<sp.tiles, kScanBlock, 0, st>>>(bins, sp.nbins, sums);
+            k_scan_tiles<<<1, kScanBlock, 0, st>>>(sums, sp.tiles, sums + sp.tiles);   // tiles <= kScanTile
+            k_scan_add<<<(sp.nbins + 255) / 256, 256, 0, st>>>(bins, sp.nbins, sums);
+            k_sort_scatter<<<gi, 256, 0, st>>>(li, ctr, in, keys, bins, sorted);
+            li = sorted;
+            *kernels += 5;
+        }
         decltype(&k_mixed<true, true, true>) kern;
         if (mb.legacy_coll) {
             if (t.wide) kern = t.prefetch ? k_mixed<true, true, true> : k_mixed<true, false, true>;
@@ -822,6 +947,12 @@ cudaError_t run(Scratch& s, const Tuning& t, DevGrid g, uint64_t grid_gen, const
         if ((e = cudaMalloc(&s.keep, keep_bytes)) != cudaSuccess) return e;
         s.keep_cap = keep_bytes;
     }
+    if (t.sort_cells && s.sort_cap < sort_bytes(mb, n)) {
+        if (s.sort) cudaFree(s.sort);
+        s.sort = nullptr; s.sort_cap = 0;
+        if ((e = cudaMalloc(&s.sort, sort_bytes(mb, n))) != cudaSuccess) return e;
+        s.sort_cap = sort_bytes(mb, n);
+    }
     Ctrs* ctr = static_cast<Ctrs*>(s.ctrs);
     if ((e = cudaMemsetAsync(ctr, 0, sizeof(Ctrs), st)) != cudaSuccess) return e;
     uint64_t* kph = static_cast<uint64_t*>(s.keep);
@@ -836,7 +967,7 @@ cudaError_t run(Scratch& s, const Tuning& t, DevGrid g, uint64_t grid_gen, const
     if (graph) {
         const uint64_t key[6] = {(uint64_t)(uintptr_t)s.lists, (uint64_t)n, launches, ((uint64_t)chunk << 32) | last_chunk,
                                  (uint64_t)(uintptr_t)io.x ^ ((uint64_t)t.blocks_per_sm << 56) ^ ((uint64_t)t.prefetch << 60) ^
-                                     ((uint64_t)t.wide << 61),
+                                     ((uint64_t)t.wide << 61) ^ ((uint64_t)t.sort_cells << 63),
                                  (uint64_t)(uintptr_t)s.nodes ^ ((uint64_t)mb.legacy_coll << 62)};
         cudaGraph_t gr = nullptr;
         if ((e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return e;

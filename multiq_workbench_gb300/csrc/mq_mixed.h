@@ -45,6 +45,7 @@ struct Tuning {
     int prefetch = 0;          // L1-prefetch the cell an ion is heading for
     int wide = 0;              // 64-byte node records read with 256-bit loads (else 48-byte records)
     uint32_t max_launches = 0; // cap on launches per call (0 = as many as the step budget needs)
+    int sort_cells = 0;        // put each launch's live list in the Morton order of the ions' cells
     int sms = 0;               // filled from the device
 };
 
@@ -61,6 +62,8 @@ struct Scratch {
     size_t nodes_cap = 0;
     uint64_t nodes_gen = ~0ull; // grid generation the records were packed from
     int nodes_stride = 0;       // float4 per record of the packed records
+    void* sort = nullptr;      // cell sort: bin counts, tile totals, keys and the sorted list
+    size_t sort_cap = 0;
     cudaGraphExec_t graph = nullptr;
     uint64_t graph_key[6] = {0, 0, 0, 0, 0, 0};
     cudaEvent_t ev[2] = {nullptr, nullptr};

@@ -128,6 +128,30 @@ def test_config1_mass_scan(grid_0p1, half_kick):
           f"mixed {list(om.transmitted)} FP64 {list(o64.transmitted)}")
 
 
+def test_config1_fig4_legacy_physics(grid_0p1):
+    """The reference's own legacy mass scan (chsim legacy-fig4: m/z 475..525 step 2 of 5+ ions, 1,000
+    each, every legacy switch: half kick, stationary-gas collisions, nearest-node fields, point-and-cone
+    launch, legacy criteria): FP64 = oracle bit for bit on every ion; mixed vs FP64 at 95%."""
+    mq = _mq()
+    from multiq_workbench_gb300 import chsim as CH
+    ph = mq.Physics.legacy(1e-3 * 133.322)
+    jobs = CH.fig4_jobs(1000)
+    n = sum(j.n for j in jobs)
+    with mq.Engine(grid_0p1, mq.PREC_F64) as e:
+        ions = mq.IonStates.empty(n)
+        o64 = e.run_batch(jobs, CH.FIG4_DC, ph, ions_out=ions)
+    from oracle import mqref as R
+    g = grid_0p1.geom
+    G = R.Grid3(grid_0p1.nx, grid_0p1.ny, grid_0p1.nz, grid_0p1.h, grid_0p1.rf, grid_0p1.ac, grid_0p1.dc_field(CH.FIG4_DC))
+    b = R.batch(ph, jobs[0].drive.v_rf, jobs[0].drive.f_rf, g.axis(), g.layers())
+    s = R.inject(b, jobs, n)
+    R.run(G, b, jobs, s)
+    _bitequal(ions, s, "Fig. 4 legacy scan FP64 vs oracle")
+    with mq.Engine(grid_0p1, mq.PREC_MIXED) as e:
+        om = e.run_batch(jobs, CH.FIG4_DC, ph)
+    _gate("config 1 Fig. 4 legacy physics", om, o64)
+
+
 @pytest.mark.parametrize("h_mm", [0.1, 0.05, 0.1 / 3.0], ids=["0.100mm", "0.050mm", "0.0333mm"])
 def test_config3_grid_study(built, h_mm):
     """The config-0 launch (half-kick rule) on a grid solved on the GPU at 0.100 / 0.050 / 0.0333 mm

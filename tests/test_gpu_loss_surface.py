@@ -57,7 +57,9 @@ def test_mixed_crossing_matches_fp64_within_an_fp32_ulp(coarse, legacy_criteria)
     # FP64: exactly the ions beyond each plane have left through it
     assert np.array_equal(a.status[:m] == 3, off > 0)
     assert np.array_equal(a.status[m:] == 2, off < 0)
-    assert ((a.status == 0) | (a.status == 2) | (a.status == 3)).all()
+    # the rest stay alive, or (legacy exit plane at 23.7 mm, beyond this grid's last node layer at
+    # 23.6 mm) leave the box just short of the plane
+    assert np.isin(a.status, (0, 2, 3, 4)).all()
     # the mixed engine classifies every ion as the FP64 kernel does
     diff = np.nonzero(a.status != b.status)[0]
     assert len(diff) == 0, (len(diff), diff[:8], a.status[diff[:8]], b.status[diff[:8]])

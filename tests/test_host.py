@@ -147,3 +147,18 @@ def test_noalloc_entry_refuses_bad_jobs_and_physics(built):
     for bad in (dict(temp_k=0.0), dict(pressure_pa=-1.0), dict(t_max=-1e-6), dict(dt=0.0)):
         assert call([mq.Job(sp, drive, 4, 1)], dataclasses.replace(good, **bad)) == -1, bad
     assert call([mq.Job(sp, drive, 2, 1), mq.Job(sp, mq.RfAc(90.0, 500e3, 0.5, 1e5), 2, 2)], good) == -5
+
+
+def test_hash_ions_is_fnv1a_over_the_fields(built):
+    """check.hash_ions (native FNV-1a 64, check.rs:95-99) equals the byte-by-byte definition."""
+    import multiq_workbench_gb300 as mq
+    from multiq_workbench_gb300 import check
+    ions = mq.IonStates.empty(300)
+    rng = np.random.default_rng(11)
+    for name, _ in mq.channel.ION_FIELDS:
+        a = getattr(ions, name)
+        a.view(np.uint8)[:] = rng.integers(0, 256, a.nbytes, dtype=np.uint8)
+    h = 1469598103934665603
+    for b in b"".join(np.ascontiguousarray(getattr(ions, n)).tobytes() for n, _ in mq.channel.ION_FIELDS):
+        h = ((h ^ b) * 1099511628211) & 0xFFFFFFFFFFFFFFFF
+    assert check.hash_ions(ions) == h
