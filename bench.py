@@ -108,6 +108,19 @@ def grid_workload(ions_per_job: int = 1000, njobs: int = 1024):
     return jobs, ph, [0.0, 5.0, -5.0, 0.0]
 
 
+def apply_tuning(eng, args) -> None:
+    """Launch-shape overrides from the command line (--chunk, --sort-cells, --no-graph)."""
+    kw = {}
+    if args.chunk:
+        kw["chunk"] = args.chunk
+    if args.sort_cells:
+        kw["sort_cells"] = True
+    if args.no_graph:
+        kw["use_graph"] = False
+    if kw:
+        eng.set_tuning(**kw)
+
+
 def run_gridstudy(args, rank: int, world: int):
     """Config 3: the same launch on grids solved at 0.100, 0.050 and 0.0333 mm (on the GPU), the
     mixed engine timed on each, the FP64 kernel run on the same ions for counts and per-ion
@@ -128,15 +141,17 @@ def run_gridstudy(args, rank: int, world: int):
     grids = []
     clocks = Clocks(local)
     value = None
-    for h in GRID_SPACINGS:
+    spacings = [h for h in GRID_SPACINGS if not args.grid or abs(h - args.grid) < 1e-4]
+    for h in spacings:
         t0 = time.perf_counter()
         f = mq.Fields.build(mq.Geom.with_spacing(h), bases=[0, 1, 3, 4], cache=False, device=local)
         t_solve = time.perf_counter() - t0
         with mq.Engine(f, mq.PREC_MIXED, device=local) as eng:
+            apply_tuning(eng, args)
             tuned = eng.tuning()   # the default launch shape (a sampled autotune picks worse ones here)
             for _ in range(args.warmup):
                 eng.run_batch(table, dc, ph)
-            if h == GRID_SPACINGS[-1]:
+            if h == spacings[-1]:
                 clocks.start()
             ms, steps = [], 0
             walls = []
@@ -210,7 +225,7 @@ def run_gridstudy(args, rank: int, world: int):
 LEGACY_METRIC = "ion-steps/s, 1 GB300: legacy Fig. 4 mass scan (legacy collisions), mixed precision vs plain FP64"
 
 
-def legacy_workload(replicas: int = 40):
+def legacy_workload(replicas: int = 8):
     """The reference's legacy Fig. 4 scan (chsim legacy-fig4): m/z 475..525 step 2 (26 values) of 5+
     ions (mass 5 m/z), 100 V / 500 kHz RF, 0.5 V / 100 kHz excitation, DC [0, +5, -5, 0] V, every
     legacy switch (half kick, stationary-gas collisions every mean free path, nearest-node fields,
@@ -225,7 +240,7 @@ def legacy_workload(replicas: int = 40):
 
 
 def run_legacy(args, rank: int, world: int):
-    """The legacy-collision path: the Fig. 4 scan x 40 seed sets (1,040,000 ions) on the 0.100 mm grid,
+    """The legacy-collision path: the Fig. 4 scan x 8 seed sets (208,000 ions) on the 0.100 mm grid,
     the mixed engine timed (``k_mixed`` with legacy collisions), the FP64 kernel on one seed set
     (26,000 ions) for the speed ratio and the class counts, and the CPU oracle on a sample."""
     import torch
@@ -235,13 +250,14 @@ def run_legacy(args, rank: int, world: int):
     ge.build()
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
-    jobs, ph, dc = legacy_workload()
+    jobs, ph, dc = legacy_workload(args.replicas)
     if rank:
         jobs = [mq.Job(j.sp, j.drive, j.n, j.seed + rank_seed0(rank)) for j in jobs]
     f = mq.Fields.build(mq.Geom(), bases=[0, 1, 3, 4], cache=False, device=local)
     table = mq.JobTable.from_jobs(jobs, pinned=True)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
     eng = mq.Engine(f, mq.PREC_MIXED, device=local)
+    apply_tuning(eng, args)
     tuned = eng.tuning()
     for _ in range(args.warmup):
         eng.run_batch(table, dc, ph)
@@ -297,7 +313,7 @@ def run_legacy(args, rank: int, world: int):
     line = {"metric": LEGACY_METRIC, "value": steps_all / t_dev, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-            "config": {"workload": f"legacy Fig. 4 scan: 26 m/z (475-525) x 1,000 ions x 40 seed sets "
+            "config": {"workload": f"legacy Fig. 4 scan: 26 m/z (475-525) x 1,000 ions x {args.replicas} seed sets "
                                    f"({table.total_ions():,} ions), Physics::legacy(1 mTorr), 0.100 mm grid",
                        "l2_flush": "256 MB write before every timed step", "tuning": tuned},
             "ion_steps_per_step": steps / args.steps,
@@ -495,8 +511,20 @@ def tandem_setup(args, rank: int = 0, precision: int = 1, grids=None):
 
 
 def tandem_bytes(st, kind: str = "mixed") -> float:
+    """Corner bytes the FP64 kernel gathers per track-step (it reads every corner every step)."""
     b = TANDEM_BYTES[kind]
     return b["cube"] * st.steps_cube + b["port"] * st.steps_port + b["idle"] * st.steps_idle
+
+
+TRACK_STATE_BYTES = 68 + 56   # k_tm_step: a track's working state read and written once per launch
+
+
+def tandem_moved(st, tracks: int) -> float:
+    """Bytes the mixed tandem's step kernel must move, from its own counters: cell-cache fills (cube:
+    8 x 32-byte records; port: 8 x 48-byte records) plus every track's state once per launch (the
+    advance's launches are a load, a store, and a bucket + step pair per 256-step chunk)."""
+    chunks = max((st.launches - 2) // 2, 0)
+    return st.cell_fills_cube * 8 * 32 + st.cell_fills_port * 8 * 48 + float(tracks) * TRACK_STATE_BYTES * chunks
 
 
 def tandem_cpu(m, pulse, steps: int, target_s: float, threads: int) -> dict:
@@ -593,7 +621,8 @@ def run_tandem(args, rank: int, world: int):
     peaks = measured_peaks()
     hbm = peaks.get("hbm_gbs") or 6800.0
     l2 = l2_read_gbs(local)
-    achieved = sum(tandem_bytes(s) for s in sts) / (sum(s.kernel_ms for s in sts) * 1e-3) / 1e9
+    achieved = sum(tandem_moved(s, args.tracks) for s in sts) / (sum(s.kernel_ms for s in sts) * 1e-3) / 1e9
+    fills = sum(s.cell_fills_cube + s.cell_fills_port for s in sts) / max(sum(s.track_steps for s in sts), 1)
     f = m.frame()
     cnt = m.counts_array()
     extra = {}
@@ -635,7 +664,10 @@ def run_tandem(args, rank: int, world: int):
             "gpu_launches": int(sum(s.launches for s in sts)),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                          "traffic": None, "peak_source": "measured hbm_gbs" if peaks.get("hbm_gbs") else "fallback",
-                         "kernel": "k_tm_step", "algorithmic_bytes_per_track_step": TANDEM_BYTES["mixed"]},
+                         "kernel": "k_tm_step",
+                         "algorithmic_bytes": "cell fills counted by the kernel x 8 records (cube 32 B, port 48 B) + "
+                                              f"{TRACK_STATE_BYTES} B per track per 256-step launch",
+                         "cell_fills_per_track_step": fills},
             "roofline_l2": {"achieved": achieved, "peak": l2, "unit": "GB/s", "frac": achieved / l2 if l2 else None,
                             "peak_source": "L2 read bandwidth measured in this run (mq_measure_l2_read_gbs)"},
             "cpu_baseline": cpu, "clocks": clk,
@@ -665,6 +697,11 @@ def main():
                     help="sweep: the batched channel sweep (default); tandem: the nine-channel tandem transport; "
                          "gridstudy: one launch on grids solved at 0.100 / 0.050 / 0.0333 mm; legacy: the Fig. 4 "
                          "mass scan with every legacy switch (legacy collisions)")
+    ap.add_argument("--chunk", type=int, default=0, help="steps per launch of the mixed engine (0 = its tuning)")
+    ap.add_argument("--sort-cells", action="store_true", help="Morton cell order of every launch's live list")
+    ap.add_argument("--no-graph", action="store_true", help="issue a multi-launch sequence without a CUDA graph")
+    ap.add_argument("--grid", type=float, default=0.0, help="gridstudy: only the grid of this spacing [mm]")
+    ap.add_argument("--replicas", type=int, default=8, help="legacy: seed sets of the 26 x 1,000-ion scan")
     ap.add_argument("--tracks", type=int, default=1 << 20, help="tandem: tracks in the pulse")
     ap.add_argument("--tandem-steps", type=int, default=1000, help="tandem: global steps per bench step")
     ap.add_argument("--port-h", type=float, default=0.05, help="tandem: port grid spacing [mm]")
@@ -728,6 +765,9 @@ def main():
     tuned = None
     if not args.no_tune:
         tuned, _ = eng.autotune(jobs, dc, ph, sample_per_job=64)
+    apply_tuning(eng, args)
+    if tuned is not None:
+        tuned = eng.tuning()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
 
     table = mq.JobTable.from_jobs(jobs, pinned=True)   # the batch's host-side input, packed once

@@ -136,6 +136,8 @@ typedef struct mq_tandem_stats {
     double kernel_ms;
     uint32_t launches, pad;
     uint64_t h2d_bytes, d2h_bytes;
+    uint64_t cell_fills_cube;   /* mixed engine: cell-cache fills in the cube (8 x 32-byte records)   */
+    uint64_t cell_fills_port;   /* mixed engine: cell-cache fills in the ports (8 x 48-byte records)  */
 } mq_tandem_stats;
 
 /* advance tracks (host arrays, in place) by `steps` global steps starting at global step

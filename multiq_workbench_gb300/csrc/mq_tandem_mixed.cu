@@ -183,6 +183,7 @@ struct TCell {
     int32_t ci, cj, ck, reg;
     float fci, fcj, fck;                // the cell as floats (no int -> float conversion per step)
     uint32_t mask;                      // port: conductor bit per corner
+    uint32_t fills_cube, fills_port;    // cache fills of this lane (cube: 8 x 32-byte records; port: 8 x 48)
 };
 
 // Constants of the track's current region, held in registers and refreshed only when the track
@@ -257,6 +258,7 @@ __device__ __forceinline__ void cell_for(const RegK& k, int reg, const float xh[
             }
         }
         c.mask = m;
+        if (k.cube) ++c.fills_cube; else ++c.fills_port;
         c.ci = ci; c.cj = cj; c.ck = ck; c.reg = reg;
         c.fci = (float)ci; c.fcj = (float)cj; c.fck = (float)ck;
     }
@@ -348,7 +350,7 @@ __global__ void __launch_bounds__(128, 3) k_tm_step(TMConst C, MTracks M, uint32
     }
     __syncthreads();
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    uint32_t n_cube = 0, n_port = 0, n_idle = 0;
+    uint32_t n_cube = 0, n_port = 0, n_idle = 0, f_cube = 0, f_port = 0;
     if (t < off[kBuckets]) {
         int r0 = 0;
         while (r0 < kBuckets - 1 && t >= off[r0 + 1]) ++r0;
@@ -369,6 +371,7 @@ __global__ void __launch_bounds__(128, 3) k_tm_step(TMConst C, MTracks M, uint32
         TCell c;
         c.ci = c.cj = c.ck = -1;
         c.reg = -1;
+        c.fills_cube = c.fills_port = 0;
         c.fci = c.fcj = c.fck = __int_as_float(0x7fc00000);
         cell_for(rk, reg, xh, c);
         uint4 rc = make_uint4(0, 0, 0, 0);
@@ -548,15 +551,21 @@ __global__ void __launch_bounds__(128, 3) k_tm_step(TMConst C, MTracks M, uint32
         }
         M.region[id] = reg;
         M.last[id] = last;
+        f_cube = c.fills_cube;
+        f_port = c.fills_port;
     }
     // executed track-steps by region kind: one atomic per warp (every lane reaches this point)
     n_cube = __reduce_add_sync(FULL, n_cube);
     n_port = __reduce_add_sync(FULL, n_port);
     n_idle = __reduce_add_sync(FULL, n_idle);
+    f_cube = __reduce_add_sync(FULL, f_cube);
+    f_port = __reduce_add_sync(FULL, f_port);
     if ((threadIdx.x & 31) == 0) {
         if (n_cube) atomicAdd(stepc + 0, (unsigned long long)n_cube);
         if (n_port) atomicAdd(stepc + 1, (unsigned long long)n_port);
         if (n_idle) atomicAdd(stepc + 2, (unsigned long long)n_idle);
+        if (f_cube) atomicAdd(stepc + 3, (unsigned long long)f_cube);
+        if (f_port) atomicAdd(stepc + 4, (unsigned long long)f_port);
     }
 }
 

@@ -311,6 +311,8 @@ class TandemStats:
     launches: int
     h2d_bytes: int
     d2h_bytes: int
+    cell_fills_cube: int = 0   # mixed engine: cell-cache fills in the cube (8 x 32-byte records)
+    cell_fills_port: int = 0   # mixed engine: cell-cache fills in the ports (8 x 48-byte records)
 
     @property
     def track_steps(self) -> int:
@@ -319,7 +321,7 @@ class TandemStats:
     @classmethod
     def from_native(cls, s: N.mq_tandem_stats) -> "TandemStats":
         return cls(int(s.steps_cube), int(s.steps_port), int(s.steps_idle), float(s.kernel_ms), int(s.launches),
-                   int(s.h2d_bytes), int(s.d2h_bytes))
+                   int(s.h2d_bytes), int(s.d2h_bytes), int(s.cell_fills_cube), int(s.cell_fills_port))
 
 
 # ---------------------------------------------------------------------------------------- model

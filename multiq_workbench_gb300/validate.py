@@ -170,6 +170,29 @@ def compare_jobs(a_jobs: list, b_jobs: list) -> dict:
     return {"chi2": stat, "dof": dof, "p": chi2_sf(stat, dof), "jobs": len(a_jobs)}
 
 
+def compare_paired(a_status, b_status) -> dict:
+    """Per-ion final classes of two engines run from the same launch draws (``a_status``,
+    ``b_status``: status arrays of equal length): the fraction of ions in the same class and
+    Bowker's test of symmetry of the class-transition table, sum over class pairs i < j of
+    (n_ij - n_ji)^2 / (n_ij + n_ji), one degree of freedom per pair seen.  With independent random
+    streams and no bias between the engines, an ion moves from class i to j as often as from j to i."""
+    import numpy as np
+    a = np.asarray(a_status).astype(np.int64)
+    b = np.asarray(b_status).astype(np.int64)
+    k = int(max(a.max(initial=0), b.max(initial=0))) + 1
+    t = np.zeros((k, k), np.int64)
+    np.add.at(t, (a, b), 1)
+    stat, dof = 0.0, 0
+    for i in range(k):
+        for j in range(i + 1, k):
+            m = t[i, j] + t[j, i]
+            if m:
+                stat += (t[i, j] - t[j, i]) ** 2 / m
+                dof += 1
+    return {"agree": float((a == b).mean()) if len(a) else 1.0, "bowker": stat, "dof": dof, "p": chi2_sf(stat, dof),
+            "table": t.tolist()}
+
+
 CLASSES = ("crashed", "returned", "transmitted", "left", "timeout")
 
 

@@ -73,12 +73,18 @@ def _bitequal(a, b, what):
         assert len(bad) == 0, f"{what}: {k} differs in {len(bad)} ions (first {bad[:5]})"
 
 
-def _gate(name, om, o64):
-    """One chi-square over the outcome classes (p >= 0.05); prints the table with per-class pulls."""
+def _gate(name, om, o64, st_m=None, st_64=None):
+    """One chi-square over the outcome classes (p >= 0.05); prints the table with per-class pulls and,
+    given both engines' per-ion statuses, the per-ion class agreement and Bowker's symmetry test of
+    the class transitions (reported, not gated)."""
     from multiq_workbench_gb300 import validate as V
     r = V.compare_classes(V.class_counts(om), V.class_counts(o64))
     pulls = ", ".join(f"{k} {c['a']}/{c['b']} ({c['pull']:+.2f})" for k, c in r["classes"].items())
-    print(f"\nPARITY {name}: chi2 {r['chi2']:.2f} dof {r['dof']} p {r['p']:.3f}; mixed/FP64: {pulls}")
+    paired = ""
+    if st_m is not None:
+        q = V.compare_paired(st_64, st_m)
+        paired = f"; per ion: {q['agree'] * 100:.1f}% same class, Bowker {q['bowker']:.2f} dof {q['dof']} p {q['p']:.3f}"
+    print(f"\nPARITY {name}: chi2 {r['chi2']:.2f} dof {r['dof']} p {r['p']:.3f}; mixed/FP64: {pulls}{paired}")
     assert r["p"] >= P_MIN, (name, r)
     return r
 
@@ -100,9 +106,10 @@ def test_config0_single_channel(grid_0p1, half_kick):
     _bitequal(ions, _oracle(grid_0p1, jobs, ph), "config 0 FP64 vs oracle")
     assert (ions.status != 0).all()
     with mq.Engine(grid_0p1, mq.PREC_MIXED) as e:
-        om = e.run_batch(jobs, DC, ph)
+        im = mq.IonStates.empty(1000)
+        om = e.run_batch(jobs, DC, ph, ions_out=im)
     assert int(om.n.sum()) == 1000
-    _gate(f"config 0 {'half-kick' if half_kick else 'corrected'}", om, o64)
+    _gate(f"config 0 {'half-kick' if half_kick else 'corrected'}", om, o64, im.status, ions.status)
 
 
 @pytest.mark.parametrize("half_kick", [False, True], ids=["corrected", "half_kick"])
@@ -120,12 +127,13 @@ def test_config1_mass_scan(grid_0p1, half_kick):
         o64 = e.run_batch(jobs, DC, ph, ions_out=ions)
     _bitequal(ions, _oracle(grid_0p1, jobs, ph), "config 1 FP64 vs oracle")
     with mq.Engine(grid_0p1, mq.PREC_MIXED) as e:
-        om = e.run_batch(jobs, DC, ph)
+        im = mq.IonStates.empty(n)
+        om = e.run_batch(jobs, DC, ph, ions_out=im)
     assert list(om.n) == [1000] * 25
-    _gate(f"config 1 {'half-kick' if half_kick else 'corrected'}", om, o64)
+    _gate(f"config 1 {'half-kick' if half_kick else 'corrected'}", om, o64, im.status, ions.status)
     pj = V.compare_jobs([V.class_counts(om, [j]) for j in range(25)], [V.class_counts(o64, [j]) for j in range(25)])
     print(f"PARITY config 1 per-job: chi2 {pj['chi2']:.1f} dof {pj['dof']} p {pj['p']:.3f}; transmitted per m/z "
-          f"mixed {list(om.transmitted)} FP64 {list(o64.transmitted)}")
+          f"mixed {[int(x) for x in om.transmitted]} FP64 {[int(x) for x in o64.transmitted]}")
 
 
 def test_config1_fig4_legacy_physics(grid_0p1):
@@ -148,8 +156,9 @@ def test_config1_fig4_legacy_physics(grid_0p1):
     R.run(G, b, jobs, s)
     _bitequal(ions, s, "Fig. 4 legacy scan FP64 vs oracle")
     with mq.Engine(grid_0p1, mq.PREC_MIXED) as e:
-        om = e.run_batch(jobs, CH.FIG4_DC, ph)
-    _gate("config 1 Fig. 4 legacy physics", om, o64)
+        im = mq.IonStates.empty(n)
+        om = e.run_batch(jobs, CH.FIG4_DC, ph, ions_out=im)
+    _gate("config 1 Fig. 4 legacy physics", om, o64, im.status, ions.status)
 
 
 @pytest.mark.parametrize("h_mm", [0.1, 0.05, 0.1 / 3.0], ids=["0.100mm", "0.050mm", "0.0333mm"])
@@ -165,12 +174,14 @@ def test_config3_grid_study(built, h_mm):
     with mq.Engine(f, mq.PREC_F64) as e:
         ions, _ = e.run_batch_ions(sample, DC, ph)
         jobs = [_job(499.0, 1000, 100 + s) for s in range(16)]
-        o64 = e.run_batch(jobs, DC, ph)
+        i64 = mq.IonStates.empty(16_000)
+        o64 = e.run_batch(jobs, DC, ph, ions_out=i64)
     _bitequal(ions, _oracle(f, sample, ph), f"config 3 at {h_mm:.4f} mm: FP64 vs oracle")
     with mq.Engine(f, mq.PREC_MIXED) as e:
-        om = e.run_batch(jobs, DC, ph)
+        im = mq.IonStates.empty(16_000)
+        om = e.run_batch(jobs, DC, ph, ions_out=im)
     assert int(om.n.sum()) == 16_000
-    _gate(f"config 3 at {h_mm:.4f} mm", om, o64)
+    _gate(f"config 3 at {h_mm:.4f} mm", om, o64, im.status, i64.status)
     del f
 
 
@@ -192,9 +203,10 @@ def test_config4_tandem_full_pulse(built):
         m = mq.TandemModel(mq.DEFAULT_TONES, n=n, seed=486, fine=True, mouth_start=True, port_grids=grids,
                            precision=prec, device=0)
         m.advance(1000)
-        res[prec] = (m.counts_array().astype(np.int64), np.bincount(m.tracks.region, minlength=14))
+        res[prec] = (m.counts_array().astype(np.int64), np.bincount(m.tracks.region, minlength=14), m.tracks.region.copy())
         m.close()
-    (c64, r64), (cm, rm) = res[mq.PREC_F64], res[mq.PREC_MIXED]
+    (c64, r64, g64), (cm, rm, gm) = res[mq.PREC_F64], res[mq.PREC_MIXED]
+    q = V.compare_paired(g64, gm)
     assert r64.sum() == n and rm.sum() == n
     reg = V.compare_classes({str(k): int(rm[k]) for k in range(14)}, {str(k): int(r64[k]) for k in range(14)})
     cols = {"entered": 0, "returned": 1, "forwarded": 2, "lost": 15}
@@ -211,7 +223,8 @@ def test_config4_tandem_full_pulse(built):
                 worst = (z, f"port {p + 1} {name} {a}/{b}")
     p_ports = V.chi2_sf(stat, dof)
     print(f"\nPARITY config 4 regions: chi2 {reg['chi2']:.2f} dof {reg['dof']} p {reg['p']:.3f}; mixed/FP64 "
-          f"{[(k, c['a'], c['b']) for k, c in reg['classes'].items()]}")
+          f"{[(k, c['a'], c['b']) for k, c in reg['classes'].items()]}; per track: {q['agree'] * 100:.1f}% same region, "
+          f"Bowker {q['bowker']:.2f} dof {q['dof']} p {q['p']:.3f}")
     print(f"PARITY config 4 ports: chi2 {stat:.2f} dof {dof} p {p_ports:.3f}; largest pull {worst[0]:+.2f} ({worst[1]}); "
           f"totals mixed {cm[:, list(cols.values())].sum(0).tolist()} FP64 {c64[:, list(cols.values())].sum(0).tolist()}")
     assert reg["p"] >= P_MIN, reg

@@ -51,3 +51,14 @@ def test_class_comparison_is_the_contingency_chi2():
     assert V.compare_classes({"crashed": 5}, {"crashed": 5})["dof"] == 0
     j = V.compare_jobs([a, a], [b, a])
     assert math.isclose(j["chi2"], r["chi2"]) and j["dof"] == 6
+
+
+def test_paired_comparison_is_bowkers_symmetry_test():
+    import numpy as np
+    a = np.array([1, 1, 2, 2, 2, 3, 3, 1, 2, 3])
+    b = np.array([1, 2, 2, 1, 1, 3, 2, 1, 2, 3])
+    r = V.compare_paired(a, b)
+    # off-diagonal pairs: (1,2): n12 = 1, n21 = 2; (2,3): n23 = 0, n32 = 1
+    assert math.isclose(r["bowker"], (1 - 2) ** 2 / 3 + (0 - 1) ** 2 / 1) and r["dof"] == 2
+    assert math.isclose(r["agree"], 0.6)
+    assert V.compare_paired(a, a)["p"] == 1.0 and V.compare_paired(a, a)["dof"] == 0
