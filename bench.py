@@ -219,28 +219,31 @@ def run_gridstudy(args, rank: int, world: int):
                             "frac": fin["mixed"]["roofline_l2_frac"],
                             "peak_source": "L2 read bandwidth measured in this run (mq_measure_l2_read_gbs)"},
             "cpu_baseline": None, "clocks": clk, "grids": grids}
-    print(json.dumps(line), flush=True)
+    return line
 
 
 LEGACY_METRIC = "ion-steps/s, 1 GB300: legacy Fig. 4 mass scan (legacy collisions), mixed precision vs plain FP64"
 
 
-def legacy_workload(replicas: int = 8):
+def legacy_workload(replicas: int = 16):
     """The reference's legacy Fig. 4 scan (chsim legacy-fig4): m/z 475..525 step 2 (26 values) of 5+
     ions (mass 5 m/z), 100 V / 500 kHz RF, 0.5 V / 100 kHz excitation, DC [0, +5, -5, 0] V, every
     legacy switch (half kick, stationary-gas collisions every mean free path, nearest-node fields,
     point-and-cone launch, legacy criteria), 1 mTorr; 1,000 ions per m/z, replicated over ``replicas``
-    seed sets to fill the GPU (26,000 x replicas ions)."""
+    seed sets to fill the GPU (26,000 x replicas ions); at most 20,000 steps of 100 ns per ion, the
+    step cap of every benchmark configuration (the preset's 1 s would let single ions run 10^7 steps)."""
     import multiq_workbench_gb300 as mq
     from multiq_workbench_gb300 import chsim as CH
     mzs = [475.0 + 2.0 * i for i in range(26)]
     jobs = [mq.Job(mq.Species(mz * 5.0, 5.0, 0.0), CH.FIG4_DRIVE, 1000, 1000 * r + int(mz))
             for r in range(replicas) for mz in mzs]
-    return jobs, mq.Physics.legacy(1e-3 * 133.322), list(CH.FIG4_DC)
+    ph = mq.Physics.legacy(1e-3 * 133.322)
+    ph.t_max = 20000 * ph.dt
+    return jobs, ph, list(CH.FIG4_DC)
 
 
 def run_legacy(args, rank: int, world: int):
-    """The legacy-collision path: the Fig. 4 scan x 8 seed sets (208,000 ions) on the 0.100 mm grid,
+    """The legacy-collision path: the Fig. 4 scan x 16 seed sets (416,000 ions, <= 20,000 steps) on the 0.100 mm grid,
     the mixed engine timed (``k_mixed`` with legacy collisions), the FP64 kernel on one seed set
     (26,000 ions) for the speed ratio and the class counts, and the CPU oracle on a sample."""
     import torch
@@ -314,7 +317,7 @@ def run_legacy(args, rank: int, world: int):
             "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
             "config": {"workload": f"legacy Fig. 4 scan: 26 m/z (475-525) x 1,000 ions x {args.replicas} seed sets "
-                                   f"({table.total_ions():,} ions), Physics::legacy(1 mTorr), 0.100 mm grid",
+                                   f"({table.total_ions():,} ions), Physics::legacy(1 mTorr), <=20000 steps, 0.100 mm grid",
                        "l2_flush": "256 MB write before every timed step", "tuning": tuned},
             "ion_steps_per_step": steps / args.steps,
             "e2e": {"value": steps_all / t_wall, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
@@ -327,7 +330,7 @@ def run_legacy(args, rank: int, world: int):
             "cpu_baseline": cpu, "clocks": clk,
             "outcomes": {k: int(getattr(out, k).sum()) for k in V.CLASSES}}
     line.update(extra)
-    print(json.dumps(line), flush=True)
+    return line
 
 
 class Clocks:
@@ -678,8 +681,8 @@ def run_tandem(args, rank: int, world: int):
                       "retry_matrix": cnt[:, 5:14].tolist(), "reverse_entries": int(cnt[:, 14].sum()),
                       "lost": cnt[:, 15].tolist(), "by_charge": cnt[:, 16:21].sum(0).tolist()}}
     line.update(extra)
-    print(json.dumps(line), flush=True)
     m.close()
+    return line
 
 
 def main():
@@ -701,7 +704,9 @@ def main():
     ap.add_argument("--sort-cells", action="store_true", help="Morton cell order of every launch's live list")
     ap.add_argument("--no-graph", action="store_true", help="issue a multi-launch sequence without a CUDA graph")
     ap.add_argument("--grid", type=float, default=0.0, help="gridstudy: only the grid of this spacing [mm]")
-    ap.add_argument("--replicas", type=int, default=8, help="legacy: seed sets of the 26 x 1,000-ion scan")
+    ap.add_argument("--replicas", type=int, default=16, help="legacy: seed sets of the 26 x 1,000-ion scan")
+    ap.add_argument("--sweep-only", action="store_true",
+                    help="default workload: print the sweep's line without the other workloads' results")
     ap.add_argument("--tracks", type=int, default=1 << 20, help="tandem: tracks in the pulse")
     ap.add_argument("--tandem-steps", type=int, default=1000, help="tandem: global steps per bench step")
     ap.add_argument("--port-h", type=float, default=0.05, help="tandem: port grid spacing [mm]")
@@ -723,7 +728,9 @@ def main():
                                   "unavailable": "the grid study's reference arm is the sweep's CPU port; run "
                                                  "--impl reference without --workload for it"}), flush=True)
         else:
-            run_gridstudy(args, rank, world)
+            line = run_gridstudy(args, rank, world)
+            if line:
+                print(json.dumps(line), flush=True)
         if dist:
             dist.barrier()
             dist.destroy_process_group()
@@ -735,13 +742,17 @@ def main():
                                   "unavailable": "the legacy scan's reference arm is the sweep's CPU port; run "
                                                  "--impl reference without --workload for it"}), flush=True)
         else:
-            run_legacy(args, rank, world)
+            line = run_legacy(args, rank, world)
+            if line:
+                print(json.dumps(line), flush=True)
         if dist:
             dist.barrier()
             dist.destroy_process_group()
         return
     if args.workload == "tandem":
-        run_tandem(args, rank, world)
+        line = run_tandem(args, rank, world)
+        if line:
+            print(json.dumps(line), flush=True)
         if dist:
             dist.barrier()
             dist.destroy_process_group()
@@ -869,11 +880,34 @@ def main():
                                                "32 MiB resident, 200 sweeps, best of 3)"},
                 "cpu_baseline": cpu, "clocks": clk, "outcomes": counts}
         line.update(extra)
-        print(json.dumps(line), flush=True)
     eng.close()
+    if rank == 0 and world == 1 and not args.sweep_only:
+        line["workloads"] = other_workloads(args)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
     if dist:
         dist.barrier()
         dist.destroy_process_group()
+
+
+def other_workloads(args) -> dict:
+    """The other measured workloads, run after the headline sweep in the default invocation so that
+    every configuration has a measured line: the grid study (config 3), the tandem (config 4) and the
+    legacy Fig. 4 scan (legacy collisions), each with 2 timed steps after 3 warm-up steps.  A
+    workload that fails is recorded with its error instead of a line."""
+    import copy
+    import gc
+    out = {}
+    for name, fn in (("gridstudy", run_gridstudy), ("tandem", run_tandem), ("legacy", run_legacy)):
+        a = copy.copy(args)
+        a.steps, a.warmup, a.workload = 2, 3, name
+        a.ions_per_job = 256
+        try:
+            out[name] = fn(a, 0, 1)
+        except Exception as e:   # keep the headline line whatever happens here
+            out[name] = {"error": f"{type(e).__name__}: {e}"}
+        gc.collect()
+    return out
 
 
 if __name__ == "__main__":

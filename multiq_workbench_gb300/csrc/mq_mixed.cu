@@ -132,7 +132,9 @@ __device__ __forceinline__ void ld256(const float4* p, float4& a, float4& b) {
         : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w) : "l"(p));
 }
 
-template <bool WIDE>
+// NEAREST (the reference's legacy field mode: the field of the cell's lowest corner, t = 0) reads
+// only that corner's record, which also holds the cell's conductor bits: one record per fill.
+template <bool WIDE, bool NEAREST>
 __device__ __forceinline__ void load_cell(const float4* __restrict__ nodes, const MixBatch& B, int32_t ci, int32_t cj,
                                           int32_t ck, Cell& c) {
     constexpr uint32_t S = WIDE ? 4u : 3u;
@@ -140,7 +142,7 @@ __device__ __forceinline__ void load_cell(const float4* __restrict__ nodes, cons
     const uint32_t base = node_of(B, ci, cj, ck);
     uint32_t m = 0;
 #pragma unroll
-    for (int q = 0; q < 8; ++q) {
+    for (int q = 0; q < (NEAREST ? 1 : 8); ++q) {
         uint32_t o = S * (base + (uint32_t)(q & 1) + ((q & 2) ? sy : 0u) + ((q & 4) ? sz : 0u));
         o = (uint32_t)MQ_CHK_SPAN(o, S, S * (size_t)sz * (size_t)B.nz, MQ_SITE_MIX_CELL);
         float4 r, d, a;
@@ -196,7 +198,7 @@ __device__ __forceinline__ float df_diff(float xh, float xl, float th, float tl)
 }
 
 // ---------------------------------------------------------------- the persistent worker
-template <bool LEGACY, bool PREFETCH, bool WIDE>
+template <bool LEGACY, bool PREFETCH, bool WIDE, bool NEAREST>
 __global__ void __launch_bounds__(128, 3)
 k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__ jobs, DevIons io,
         const uint32_t* __restrict__ list_in, uint32_t* __restrict__ list_out, Ctrs* ctr, int in_slot, uint32_t chunk,
@@ -238,7 +240,23 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
     c.ci = c.cj = c.ck = -1; c.mask = 0;
     c.fci = c.fcj = c.fck = __int_as_float(0x7fc00000);   // NaN: differs from every floored position
 
+    // Queue traffic is warp-synchronous and happens once every 4 iterations: survivors that ended in
+    // the last 4 iterations are appended to the next launch's list, then lanes without an ion are
+    // refilled (a lane that finished waits at most 3 iterations; 1.8% on the sweep and 3% on the
+    // legacy scan against ballots every iteration).
+    bool append = false;
     for (;;) {
+      if ((iter & 3u) == 0u) {
+        // ---- warp-ballot compaction of survivors into the next launch's list
+        const unsigned am = __ballot_sync(FULL, append);
+        if (am) {
+            const int leader = __ffs(am) - 1;
+            uint32_t base = 0;
+            if ((int)lane == leader) base = atomicAdd(count_out, (uint32_t)__popc(am));
+            base = __shfl_sync(FULL, base, leader);
+            if (append) list_out[MQ_CHK(base + __popc(am & ((1u << lane) - 1u)), n_all, MQ_SITE_MIX_LIST_OUT)] = id;
+        }
+        append = false;
         // ---- refill: one warp-aggregated atomic hands out queue slots to lanes without an ion
         const unsigned need = __ballot_sync(FULL, !have && !drained);
         if (need) {
@@ -270,17 +288,23 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
                     Prf = orf + (uint64_t)n * Wrf;
                     Pac = oac + (uint64_t)n * Wac;
                     // drive state as an uninterrupted run has it: exact at the last step that is
-                    // a multiple of 4, then rotated forward (so re-queued ions continue bitwise)
-                    {
-                        const uint32_t r4 = n & 3u;
+                    // a multiple of 4, then rotated forward (so re-queued ions continue bitwise).
+                    // An ion at a multiple of 4 steps (every fresh ion) first steps on a re-sync
+                    // iteration, which sets its drive exactly and draws its next Philox block, so
+                    // neither is done here for it
+                    const uint32_t r4 = n & 3u;
+                    if (r4) {
                         turn_sincos(Prf - (uint64_t)r4 * Wrf, srf, crf);
                         turn_sincos(Pac - (uint64_t)r4 * Wac, sac, cac);
                         for (uint32_t q = 0; q < r4; ++q) { rotate(srf, crf, B.cw_rf, B.sw_rf); rotate(sac, cac, cw_ac, sw_ac); }
                     }
                     const uint64_t key = io.rng[id];
                     k0 = (uint32_t)key; k1 = (uint32_t)(key >> 32);
-                    if (!LEGACY) { rc = philox(k0, k1, n >> 2, 0u, 0u, 0u); rn = philox(k0, k1, (n >> 2) + 1u, 0u, 0u, 0u); }
-                    load_cell<WIDE>(nodes, B, clampi(__float2int_rd(xh[0]), 0, B.nx - 2), clampi(__float2int_rd(xh[1]), 0, B.ny - 2),
+                    if (!LEGACY) {
+                        rc = philox(k0, k1, n >> 2, 0u, 0u, 0u);
+                        if (r4) rn = philox(k0, k1, (n >> 2) + 1u, 0u, 0u, 0u);
+                    }
+                    load_cell<WIDE, NEAREST>(nodes, B, clampi(__float2int_rd(xh[0]), 0, B.nx - 2), clampi(__float2int_rd(xh[1]), 0, B.ny - 2),
                               clampi(__float2int_rd(xh[2]), 0, B.nz - 2), c);
                     ++loads;
                     done = 0;
@@ -291,8 +315,8 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
             }
         }
         if (!__any_sync(FULL, have)) break;
+      }
 
-        bool append = false;
         // A lane steps its ion only when the ion's step count is congruent to the warp's
         // iteration counter mod 4 (a freshly loaded ion waits at most 3 iterations).  Every
         // warp-uniform event below (Philox refresh and exact drive re-sync, each 4 iterations)
@@ -305,7 +329,7 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
         if (act) {
             // ---- field at the current position
             float tx = 0.f, ty = 0.f, tz = 0.f;
-            if (!B.nearest) {
+            if (!NEAREST) {
                 tx = __fadd_rn(__fsub_rn(xh[0], c.fci), xl[0]);
                 ty = __fadd_rn(__fsub_rn(xh[1], c.fcj), xl[1]);
                 tz = __fadd_rn(__fsub_rn(xh[2], c.fck), xl[2]);
@@ -314,7 +338,9 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
             const float a_ac = v_ac * sac;
             float E[3];
 #pragma unroll
-            for (int d = 0; d < 3; ++d) E[d] = field_comp(c.R[d], c.D[d], c.A[d], a_rf, a_ac, tx, ty, tz);
+            for (int d = 0; d < 3; ++d)
+                E[d] = NEAREST ? fmaf(a_rf, c.R[d][0], fmaf(a_ac, c.A[d][0], c.D[d][0]))   // = field_comp at t = 0
+                               : field_comp(c.R[d], c.D[d], c.A[d], a_rf, a_ac, tx, ty, tz);
             // ---- kick (compensated) and drift (compensated)
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
@@ -409,9 +435,9 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
             if (ffi != c.fci || ffj != c.fcj || ffk != c.fck) {
                 const int32_t ci = clampi(__float2int_rd(xh[0]), 0, B.nx - 2), cj = clampi(__float2int_rd(xh[1]), 0, B.ny - 2),
                               ck = clampi(__float2int_rd(xh[2]), 0, B.nz - 2);
-                if (ci != c.ci || cj != c.cj || ck != c.ck) { load_cell<WIDE>(nodes, B, ci, cj, ck, c); ++loads; }
+                if (ci != c.ci || cj != c.cj || ck != c.ck) { load_cell<WIDE, NEAREST>(nodes, B, ci, cj, ck, c); ++loads; }
             }
-            if (PREFETCH) {
+            if (PREFETCH && !NEAREST) {
                 const int32_t pi = clampi(__float2int_rd(xh[0] + uh[0]), 0, B.nx - 2);
                 const int32_t pj = clampi(__float2int_rd(xh[1] + uh[1]), 0, B.ny - 2);
                 const int32_t pk = clampi(__float2int_rd(xh[2] + uh[2]), 0, B.nz - 2);
@@ -450,15 +476,6 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
                 append = status == 0;
                 have = false;
             }
-        }
-        // ---- warp-ballot compaction of survivors into the next launch's list
-        const unsigned am = __ballot_sync(FULL, append);
-        if (am) {
-            const int leader = __ffs(am) - 1;
-            uint32_t base = 0;
-            if ((int)lane == leader) base = atomicAdd(count_out, (uint32_t)__popc(am));
-            base = __shfl_sync(FULL, base, leader);
-            if (append) list_out[MQ_CHK(base + __popc(am & ((1u << lane) - 1u)), n_all, MQ_SITE_MIX_LIST_OUT)] = id;
         }
     }
 #pragma unroll
@@ -833,6 +850,22 @@ void release(Scratch& s) {
     s = Scratch();
 }
 
+// the stepping kernel for the batch's physics and the tuning (the nearest-node field mode reads one
+// record per fill, so the L1 prefetch of the next cell does not apply to it)
+typedef decltype(&k_mixed<true, true, true, false>) Kernel;
+static Kernel pick_kernel(const Tuning& t, const MixBatch& mb) {
+    if (mb.nearest) {
+        if (mb.legacy_coll) return t.wide ? k_mixed<true, false, true, true> : k_mixed<true, false, false, true>;
+        return t.wide ? k_mixed<false, false, true, true> : k_mixed<false, false, false, true>;
+    }
+    if (mb.legacy_coll) {
+        if (t.wide) return t.prefetch ? k_mixed<true, true, true, false> : k_mixed<true, false, true, false>;
+        return t.prefetch ? k_mixed<true, true, false, false> : k_mixed<true, false, false, false>;
+    }
+    if (t.wide) return t.prefetch ? k_mixed<false, true, true, false> : k_mixed<false, false, true, false>;
+    return t.prefetch ? k_mixed<false, true, false, false> : k_mixed<false, false, false, false>;
+}
+
 // bins of the cell sort: the top min(22, 3 b) bits of the Morton code, b the bits of the largest
 // cell index (nbins <= 2^22, so the tile totals fit one scan tile)
 struct SortPlan {
@@ -856,7 +889,7 @@ static size_t sort_bytes(const MixBatch& mb, uint32_t n) {
     return sizeof(uint32_t) * ((size_t)p.nbins + p.tiles + 1 + 2 * (size_t)n);
 }
 
-static cudaError_t enqueue_launches(const Scratch& s, const Tuning& t, const MixBatch& mb, DevIons io,
+static cudaError_t enqueue_launches(const Scratch& s, const Tuning& t, int blocks_per_sm, const MixBatch& mb, DevIons io,
                                     uint32_t n, uint32_t launches, uint32_t chunk, uint32_t last_chunk, cudaStream_t st,
                                     uint32_t* kernels) {
     uint32_t* lists = static_cast<uint32_t*>(s.lists);
@@ -865,7 +898,7 @@ static cudaError_t enqueue_launches(const Scratch& s, const Tuning& t, const Mix
     const float4* nodes = static_cast<const float4*>(s.nodes);
     uint64_t* kph = static_cast<uint64_t*>(s.keep);
     float* keep = reinterpret_cast<float*>(kph + (size_t)2 * n);
-    const int grid = t.sms * t.blocks_per_sm;
+    const int grid = t.sms * blocks_per_sm;
     const SortPlan sp = sort_plan(mb, n);
     uint32_t* bins = static_cast<uint32_t*>(s.sort);
     uint32_t* sums = bins + sp.nbins;
@@ -888,14 +921,7 @@ static cudaError_t enqueue_launches(const Scratch& s, const Tuning& t, const Mix
             li = sorted;
             *kernels += 5;
         }
-        decltype(&k_mixed<true, true, true>) kern;
-        if (mb.legacy_coll) {
-            if (t.wide) kern = t.prefetch ? k_mixed<true, true, true> : k_mixed<true, false, true>;
-            else kern = t.prefetch ? k_mixed<true, true, false> : k_mixed<true, false, false>;
-        } else {
-            if (t.wide) kern = t.prefetch ? k_mixed<false, true, true> : k_mixed<false, false, true>;
-            else kern = t.prefetch ? k_mixed<false, true, false> : k_mixed<false, false, false>;
-        }
+        const Kernel kern = pick_kernel(t, mb);
         kern<<<grid, t.tpb, 0, st>>>(nodes, mb, jobs, io, li, lo, ctr, in, ch, keep, kph, n);
         *kernels += 2;
     }
@@ -977,17 +1003,27 @@ cudaError_t run(Scratch& s, const Tuning& t, DevGrid g, uint64_t grid_gen, const
     k_init_list<<<(n + 255) / 256, 256, 0, st>>>(io, n, static_cast<uint32_t*>(s.lists), ctr, mb, keep, kph, staged);
     info->kernel_launches += 1;
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    // resident blocks per SM: the tuning's, except for the nearest-node kernels, which hold no
+    // 8-corner cache (about 100 registers instead of 167) and run as many blocks as fit
+    int blocks = t.blocks_per_sm;
+    if (mb.nearest) {
+        int nb = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, pick_kernel(t, mb), t.tpb, 0) == cudaSuccess && nb > 0)
+            blocks = nb;
+        else
+            cudaGetLastError();
+    }
     cudaEventRecord(s.ev[0], st);
     uint32_t kernels = 0;
     const bool graph = t.use_graph && launches > 1;
     if (graph) {
         const uint64_t key[6] = {(uint64_t)(uintptr_t)s.lists, (uint64_t)n, launches, ((uint64_t)chunk << 32) | last_chunk,
-                                 (uint64_t)(uintptr_t)io.x ^ ((uint64_t)t.blocks_per_sm << 56) ^ ((uint64_t)t.prefetch << 60) ^
+                                 (uint64_t)(uintptr_t)io.x ^ ((uint64_t)blocks << 56) ^ ((uint64_t)t.prefetch << 60) ^
                                      ((uint64_t)t.wide << 61) ^ ((uint64_t)t.sort_cells << 63),
-                                 (uint64_t)(uintptr_t)s.nodes ^ ((uint64_t)mb.legacy_coll << 62)};
+                                 (uint64_t)(uintptr_t)s.nodes ^ ((uint64_t)mb.legacy_coll << 62) ^ ((uint64_t)mb.nearest << 61)};
         cudaGraph_t gr = nullptr;
         if ((e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return e;
-        enqueue_launches(s, t, mb, io, n, launches, chunk, last_chunk, st, &kernels);
+        enqueue_launches(s, t, blocks, mb, io, n, launches, chunk, last_chunk, st, &kernels);
         e = cudaStreamEndCapture(st, &gr);
         if (e != cudaSuccess) { if (gr) cudaGraphDestroy(gr); return e; }
         // re-use the instantiated graph when only kernel parameters changed
@@ -1006,7 +1042,7 @@ cudaError_t run(Scratch& s, const Tuning& t, DevGrid g, uint64_t grid_gen, const
         if ((e = cudaGraphLaunch(s.graph, st)) != cudaSuccess) return e;
         info->graph_replays = 1;
     } else {
-        if ((e = enqueue_launches(s, t, mb, io, n, launches, chunk, last_chunk, st, &kernels)) != cudaSuccess) return e;
+        if ((e = enqueue_launches(s, t, blocks, mb, io, n, launches, chunk, last_chunk, st, &kernels)) != cudaSuccess) return e;
     }
     cudaEventRecord(s.ev[1], st);
     if (write_states) {

@@ -39,7 +39,8 @@ struct MixBatch {      // per-batch constants (device-resident parameter block)
 
 struct Tuning {
     int tpb = 128;             // threads per block
-    int blocks_per_sm = 3;     // resident blocks per SM for the persistent grid (168 registers/thread; 3 at most)
+    int blocks_per_sm = 3;     // resident blocks per SM for the persistent grid (168 registers/thread; 3 at most);
+                               // the nearest-node kernels (about 100 registers) run as many as fit instead
     uint32_t chunk = 20000;    // steps per ion per launch (compaction interval)
     int use_graph = 1;         // replay the launch sequence as one CUDA graph
     int prefetch = 0;          // L1-prefetch the cell an ion is heading for

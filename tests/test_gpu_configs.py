@@ -8,9 +8,11 @@ Each configuration is run by the plain FP64 kernel and by the mixed-precision en
   ions differ one by one while the distributions must not: its outcome-class counts are held to
   the FP64 kernel's at the 95% level by one chi-square test of homogeneity per configuration and
   update rule over the outcome classes (crashed, returned, transmitted, left, timeout; classes
-  empty in both are dropped), p >= 0.05.  That single joint test per configuration is the
-  multiplicity rule: classes are not tested one by one.  Per-class pooled binomial pulls are
-  printed beside it.
+  empty in both are dropped), p >= 0.05.  Both engines start from the same launch draws, so the
+  classes are also compared ion by ion: Bowker's test of symmetry of the class-transition table
+  (an ion moves from class i to j as often as from j to i), p >= 0.05.  Those two joint tests per
+  configuration are the multiplicity rule: classes are not tested one by one.  Per-class pooled
+  binomial pulls and the per-ion agreement are printed beside them.
 
 Configurations (channel geometry solved on the GPU, 100 V / 500 kHz RF, 0.5 V / 100 kHz
 excitation, DC [0, +5, -5, 0] V, 1 mTorr N2 at 300 K, z = +1 with N2 CCS 2.95 m^(2/3) A^2,
@@ -74,9 +76,9 @@ def _bitequal(a, b, what):
 
 
 def _gate(name, om, o64, st_m=None, st_64=None):
-    """One chi-square over the outcome classes (p >= 0.05); prints the table with per-class pulls and,
-    given both engines' per-ion statuses, the per-ion class agreement and Bowker's symmetry test of
-    the class transitions (reported, not gated)."""
+    """One chi-square over the outcome classes and, given both engines' per-ion statuses, Bowker's
+    symmetry test of the class transitions (each p >= 0.05); prints both with the per-class pulls
+    and the per-ion class agreement."""
     from multiq_workbench_gb300 import validate as V
     r = V.compare_classes(V.class_counts(om), V.class_counts(o64))
     pulls = ", ".join(f"{k} {c['a']}/{c['b']} ({c['pull']:+.2f})" for k, c in r["classes"].items())
@@ -86,6 +88,8 @@ def _gate(name, om, o64, st_m=None, st_64=None):
         paired = f"; per ion: {q['agree'] * 100:.1f}% same class, Bowker {q['bowker']:.2f} dof {q['dof']} p {q['p']:.3f}"
     print(f"\nPARITY {name}: chi2 {r['chi2']:.2f} dof {r['dof']} p {r['p']:.3f}; mixed/FP64: {pulls}{paired}")
     assert r["p"] >= P_MIN, (name, r)
+    if st_m is not None:
+        assert q["p"] >= P_MIN, (name, q)
     return r
 
 
@@ -189,8 +193,9 @@ def test_config4_tandem_full_pulse(built):
     """1,048,576 tracks at the nine mouths, ports on nine device copies of the 0.050 mm S14 grid,
     1,000 global steps from the same pulse in both engines.  Gates at 95%: the per-track final
     region (split, nine ports, combiner, lost, back, detected: one multinomial chi-square over the
-    tracks), and the per-port entered / returned / forwarded / lost counters (one chi-square over the
-    36 counters, each difference scaled by its Poisson variance a + b)."""
+    tracks, and Bowker's symmetry test of the per-track region transitions), and the per-port
+    entered / returned / forwarded / lost counters (one chi-square over the 36 counters, each
+    difference scaled by its Poisson variance a + b)."""
     mq = _mq()
     from multiq_workbench_gb300 import validate as V
     h = 0.05
@@ -228,4 +233,5 @@ def test_config4_tandem_full_pulse(built):
     print(f"PARITY config 4 ports: chi2 {stat:.2f} dof {dof} p {p_ports:.3f}; largest pull {worst[0]:+.2f} ({worst[1]}); "
           f"totals mixed {cm[:, list(cols.values())].sum(0).tolist()} FP64 {c64[:, list(cols.values())].sum(0).tolist()}")
     assert reg["p"] >= P_MIN, reg
+    assert q["p"] >= P_MIN, q
     assert p_ports >= P_MIN, (stat, dof, worst)
