@@ -43,11 +43,12 @@ CORNERS = 8
 ION_STATE_BYTES = 48 + 16 + 24 + 56 + 64   # double-floats, phase offsets, counters + key, job record; write-back
 
 
-def stepping_bytes(stats, wide: bool) -> float:
+def stepping_bytes(stats, wide: bool, nearest: bool = False) -> float:
     """Algorithmic bytes of the stepping kernel(s) of one call, from the kernel's own counters: cell
-    fills x 8 node records, plus the state traffic of every ion taken from the work queue."""
+    fills x 8 node records (1 record in the nearest-node field mode, which reads only the cell's
+    lowest corner), plus the state traffic of every ion taken from the work queue."""
     rec = 64 if wide else 48
-    return float(stats.cell_loads) * CORNERS * rec + float(stats.ions_queued) * ION_STATE_BYTES
+    return float(stats.cell_loads) * (1 if nearest else CORNERS) * rec + float(stats.ions_queued) * ION_STATE_BYTES
 
 
 def cpu_model() -> str:
@@ -277,7 +278,7 @@ def run_legacy(args, rank: int, world: int):
         ms.append(st.kernel_ms)
         step_ms.append(st.step_kernel_ms)
         steps += st.ion_steps
-        moved += stepping_bytes(st, tuned["wide_records"])
+        moved += stepping_bytes(st, tuned["wide_records"], ph.legacy_fields)
         loads += st.cell_loads
         launches += st.kernel_launches
         h2d, d2h = st.h2d_bytes, st.d2h_bytes
@@ -324,7 +325,9 @@ def run_legacy(args, rank: int, world: int):
             "gpu_launches": int(launches),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                          "traffic": None, "peak_source": "measured hbm_gbs" if peaks.get("hbm_gbs") else "fallback",
-                         "kernel": "k_mixed (legacy collisions)",
+                         "kernel": "k_mixed (legacy collisions, nearest-node fields)",
+                         "algorithmic_bytes": f"cell fills counted by the kernel x 1 node record ({64 if tuned['wide_records'] else 48} B) "
+                                              f"+ {ION_STATE_BYTES} B per ion taken from the queue",
                          "cell_loads_per_ion_step": loads / max(steps, 1)},
             "roofline_l2": {"achieved": achieved, "peak": l2, "unit": "GB/s", "frac": achieved / l2 if l2 else None},
             "cpu_baseline": cpu, "clocks": clk,
