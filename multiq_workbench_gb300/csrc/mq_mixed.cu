@@ -16,7 +16,8 @@
 //     crash test), with an optional L1 prefetch of the cell the ion is heading for;
 //   * RF / AC phase as exact 64-bit fixed-point turn accumulators (phase = offset +
 //     step * f * dt mod 1), evaluated with an FP32 quarter-turn polynomial;
-//   * Philox-4x32-10 counter RNG keyed by the ion's 64-bit key, counter = step;
+//   * Philox-4x32-10 counter RNG keyed by the ion's 64-bit key, counter = step (thermal candidates
+//     and collisions) or 4-step window (legacy collisions: two blocks per window);
 //   * device injection with the FP64 injection's draws and FP32 transforms (k_inject_mixed).
 #include "mq_mixed.h"
 #include "mq_check.h"
@@ -131,6 +132,11 @@ __device__ __forceinline__ void ld256(const float4* p, float4& a, float4& b) {
     asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
         : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w) : "l"(p));
 }
+// the same without allocating the lines in L1 (they are fetched from L2 into registers)
+__device__ __forceinline__ void ld256_na(const float4* p, float4& a, float4& b) {
+    asm("ld.global.nc.L1::no_allocate.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w) : "l"(p));
+}
 
 // NEAREST (the reference's legacy field mode: the field of the cell's lowest corner, t = 0) reads
 // only that corner's record, which also holds the cell's conductor bits: one record per fill.
@@ -146,9 +152,17 @@ __device__ __forceinline__ void load_cell(const float4* __restrict__ nodes, cons
         uint32_t o = S * (base + (uint32_t)(q & 1) + ((q & 2) ? sy : 0u) + ((q & 4) ? sz : 0u));
         o = (uint32_t)MQ_CHK_SPAN(o, S, S * (size_t)sz * (size_t)B.nz, MQ_SITE_MIX_CELL);
         float4 r, d, a;
-        if (WIDE) {
+        if (WIDE && !NEAREST) {
+            // 64-byte records: both loads are 32-byte aligned. Wide records serve the grids whose
+            // fills hit L2; left out of L1 they do not evict the lines the narrow-record grids
+            // depend on either way (5% on the sweep; the fine grids' 48-byte fills lose 3x
+            // without L1, so they keep it)
             float4 spare;
-            ld256(nodes + o, r, d);        // 64-byte records: both loads are 32-byte aligned
+            ld256_na(nodes + o, r, d);
+            ld256_na(nodes + o + 2, a, spare);
+        } else if (WIDE) {
+            float4 spare;
+            ld256(nodes + o, r, d);
             ld256(nodes + o + 2, a, spare);
         } else {
             r = __ldg(nodes + o); d = __ldg(nodes + o + 1); a = __ldg(nodes + o + 2);
@@ -303,6 +317,9 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
                     if (!LEGACY) {
                         rc = philox(k0, k1, n >> 2, 0u, 0u, 0u);
                         if (r4) rn = philox(k0, k1, (n >> 2) + 1u, 0u, 0u, 0u);
+                    } else if (r4) {   // the legacy collision words of the current 4-step window
+                        rc = philox(k0, k1, n >> 2, 2u, 0u, 0u);
+                        rn = philox(k0, k1, n >> 2, 3u, 0u, 0u);
                     }
                     load_cell<WIDE, NEAREST>(nodes, B, clampi(__float2int_rd(xh[0]), 0, B.nx - 2), clampi(__float2int_rd(xh[1]), 0, B.ny - 2),
                               clampi(__float2int_rd(xh[2]), 0, B.nz - 2), c);
@@ -324,6 +341,13 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
         // results are reproducible bit for bit.
         const bool act = have && (((iter ^ n) & 3u) == 0u);
         if (!LEGACY && (iter & 3u) == 0u && act) rn = philox(k0, k1, (n >> 2) + 1u, 0u, 0u, 0u);
+        // legacy collisions draw from two Philox blocks per 4-step window, computed here with every
+        // lane of the warp active (7% on the legacy scan against one block per collision inside
+        // the divergent collision branch); a collision at window step q takes words 2q and 2q + 1
+        if (LEGACY && (iter & 3u) == 0u && act) {
+            rc = philox(k0, k1, n >> 2, 2u, 0u, 0u);
+            rn = philox(k0, k1, n >> 2, 3u, 0u, 0u);
+        }
         if ((iter & 3u) == 0u && act) { turn_sincos(Prf, srf, crf); turn_sincos(Pac, sac, cac); }
         ++iter;
         if (act) {
@@ -404,14 +428,18 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
                 leg -= 1;
                 if (leg <= 0) {
                     const float mr = sj_mr[threadIdx.x], floor_v = sj_floor[threadIdx.x], mfp_mean = sj_mfp[threadIdx.x];
-                    const uint4 r0 = philox(k0, k1, nprev, 1u, 0u, 0u);
+                    // two 32-bit words of this window step: cos(theta) from the top 24 bits of the
+                    // first, the free path from the top 24 of the second, phi from their low bytes
+                    const uint32_t q = nprev & 3u;
+                    const uint32_t wa = q == 0 ? rc.x : q == 1 ? rc.z : q == 2 ? rn.x : rn.z;
+                    const uint32_t wb = q == 0 ? rc.y : q == 1 ? rc.w : q == 2 ? rn.y : rn.w;
                     const float u2v = B.u2v_f;
                     float v[3] = {uh[0] * u2v, uh[1] * u2v, uh[2] * u2v};
                     const float vm = sqrtf(fmaf(v[0], v[0], fmaf(v[1], v[1], v[2] * v[2])));
                     if (vm > floor_v) {
-                        const float cth = 2.0f * unif(r0.x) - 1.0f;
+                        const float cth = 2.0f * unif(wa) - 1.0f;
                         float sp, cp;
-                        angle_sincos(unif(r0.y), &sp, &cp);
+                        angle_sincos(unif16(((wa & 0xffu) << 8) | (wb & 0xffu)), &sp, &cp);
                         const float sn = sqrtf(fmaxf(0.0f, 1.0f - cth * cth));
                         const float dd[3] = {sn * cp, sn * sp, cth};
                         const float v2u = B.v2u_f;
@@ -422,7 +450,7 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
                         }
                         ncoll += 1;
                     }
-                    const float mfp = -__logf(fmaxf(unif(r0.z), 1e-7f)) * mfp_mean;
+                    const float mfp = -__logf(fmaxf(unif(wb), 1e-7f)) * mfp_mean;
                     const float vn = sqrtf(fmaf(v[0], v[0], fmaf(v[1], v[1], v[2] * v[2])));
                     const float st = floorf(mfp / fmaxf(vn, 1e-3f) / B.dt_f);
                     leg = st < 1.0f ? 1 : (st < 2147483520.0f ? (int32_t)st : 2147483647);
@@ -447,14 +475,18 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
             // (the loss-surface planes - exit, return and the crash window - are crossed on the full
             // double-float position against the double-float thresholds; the box test is the
             // unclamped cell index leaving [0, n-2])
+            // A plane more than one cell away cannot be crossed whatever the low parts hold, so the
+            // exact test runs only within a cell of it; the crash window matters only in a cell with
+            // a conductor corner (most cells have none).
             int32_t status = 0;
-            if (df_diff(xh[2], xl[2], B.z_exit_h, B.z_exit_l) > 0.0f) status = 3;
-            else if (df_diff(xh[2], xl[2], B.z_ret_h, B.z_ret_l) < 0.0f) status = 2;
+            if (xh[2] > B.z_exit_near && df_diff(xh[2], xl[2], B.z_exit_h, B.z_exit_l) > 0.0f) status = 3;
+            else if (xh[2] < B.z_ret_near && df_diff(xh[2], xl[2], B.z_ret_h, B.z_ret_l) < 0.0f) status = 2;
             else if (ffi < 0.0f || ffj < 0.0f || ffk < 0.0f || ffi > B.lim_x - 1.0f || ffj > B.lim_y - 1.0f ||
                      ffk > B.lim_z - 1.0f)
                 status = 4;
             else {
-                if (df_diff(xh[2], xl[2], B.cz0_h, B.cz0_l) > 0.0f && df_diff(xh[2], xl[2], B.cz1_h, B.cz1_l) < 0.0f) {
+                if (c.mask != 0u && df_diff(xh[2], xl[2], B.cz0_h, B.cz0_l) > 0.0f &&
+                    df_diff(xh[2], xl[2], B.cz1_h, B.cz1_l) < 0.0f) {
                     const float fx = __fadd_rn(__fsub_rn(xh[0], c.fci), xl[0]);
                     const float fy = __fadd_rn(__fsub_rn(xh[1], c.fcj), xl[1]);
                     const float fz = __fadd_rn(__fsub_rn(xh[2], c.fck), xl[2]);
@@ -816,6 +848,8 @@ MixBatch make_mix_batch(const mqp::Batch& b) {
     split(b.z_return / b.h, m.z_ret_h, m.z_ret_l);
     split(b.crash_z0 / b.h, m.cz0_h, m.cz0_l);
     split(b.crash_z1 / b.h, m.cz1_h, m.cz1_l);
+    m.z_exit_near = m.z_exit_h - 1.0f;
+    m.z_ret_near = m.z_ret_h + 1.0f;
     m.lim_x = (float)(b.nx - 1);
     m.lim_y = (float)(b.ny - 1);
     m.lim_z = (float)(b.nz - 1);

@@ -30,6 +30,7 @@ struct MixBatch {      // per-batch constants (device-resident parameter block)
     float cw_rf, sw_rf;              // cos / sin of the RF phase advance per step
     float z_exit_h, z_exit_l, z_ret_h, z_ret_l;       // grid units, double-float
     float cz0_h, cz0_l, cz1_h, cz1_l;                 // crash window, grid units
+    float z_exit_near, z_ret_near;                    // one cell inside the exit / return planes
     float lim_x, lim_y, lim_z;                        // n - 1 (exact)
     int32_t nx, ny, nz;
     int32_t nearest, legacy_coll;
