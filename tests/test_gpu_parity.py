@@ -131,6 +131,25 @@ def test_mixed_deterministic(coarse):
     _assert_bitequal(a, b, "mixed run twice")
 
 
+@pytest.mark.parametrize("name", ["half_kick_gauss", "legacy_all", "legacy_coll_trilinear"])
+def test_mixed_requeue_mid_window_is_bitwise(coarse, name):
+    """Launches of 701 steps re-queue every surviving ion at a step count that is not a multiple of
+    4, so its refill rebuilds the drive state and the Philox blocks of a window already begun (the
+    thermal candidates' blocks, or the legacy collisions' two blocks per window): every ion's final
+    state equals the single-launch run's bit for bit, for thermal gas and for legacy collisions with
+    nearest-node and with trilinear fields."""
+    mq = _mq()
+    ph = _variants()[name]
+    jobs = _jobs(512, legacy_species=name.startswith("legacy"))
+    dc = [0.0, 5.0, -5.0, 0.0]
+    with mq.Engine(coarse, mq.PREC_MIXED) as e:
+        a, _ = e.run_batch_ions(jobs, dc, ph)
+        e.set_tuning(chunk=701)
+        b, _ = e.run_batch_ions(jobs, dc, ph)
+        assert e.last_stats.step_kernel_launches == 5
+    _assert_bitequal(a, b, f"{name}: 701-step launches vs one launch")
+
+
 def test_cell_sort_keeps_every_result(coarse):
     """Putting each launch's live list in the Morton order of the ions' cells (a device counting sort
     before every launch) changes only which ions share a warp: with 700-step launches (so the list is
