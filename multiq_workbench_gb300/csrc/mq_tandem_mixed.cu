@@ -6,8 +6,11 @@
 //     groups the tracks by region (splitter, nine ports, combiner), so warps start out
 //     reading one field grid (ragged batching by field id) and lost / finished tracks drop out;
 //   * position and velocity are FP32 double-floats in grid units of the track's current region
-//     (cube grid in mm, or the port's grid); region changes convert through FP64 with
-//     trapsim's enter / leave arithmetic (lib.rs:338-385);
+//     (cube grid in mm, or the port's grid); trapsim's enter / leave transforms (lib.rs:338-385)
+//     are affine maps between the grids' coordinates, applied in double-float arithmetic with
+//     double-float constants, and a port is left through the plane its double-float z crossed, so
+//     the step kernel does no FP64 arithmetic (GB300's FP64 pipe made the FP64 conversions a third
+//     of the pipe time in the chunks where most tracks change region);
 //   * fields as interleaved node records: cube {RF, region DC} 32 B (one 256-bit load), port
 //     {RF, DC (+ gate bias on idle ports), AC} 48 B with the cell's conductor bits in a spare word
 //     (64-byte port records with 256-bit loads measured 28% slower: the port grids' reloads reach
@@ -92,6 +95,11 @@ struct TMConst {
     double clo_d[3], ch_d, seam_m, axis_m, mouth_m[9][2];
     double clo_m[3], ch_m, inv_ch_m, cu2v_d, cv2u_d;   // cube origin and spacing [m], 1 / h, h / dt, dt / h
     PortM port[9];
+    // Region changes as double-float affine maps of grid coordinates, y = a x + b per axis (the same a
+    // scales the velocity): entering port i from the splitter (b[2]) or the combiner (b[3], z and its
+    // velocity reversed), and leaving it through the return plane (b[2]) or the exit plane (b[3], z
+    // reversed); zr / ze are the port's return / exit planes in its grid units
+    float2 en_a[9], en_b[9][4], lv_a[9], lv_b[9][4], zr[9], ze[9];
     float qmdt2[8], nsd[8], mr[8];   // per species: q/m dt^2 [m per V/m], n sigma dt, M/(m+M)
     float s_gas, pad1;
     double dt;
@@ -262,6 +270,23 @@ __device__ __forceinline__ void cell_for(const RegK& k, int reg, const float xh[
         c.ci = ci; c.cj = cj; c.ck = ck; c.reg = reg;
         c.fci = (float)ci; c.fcj = (float)cj; c.fck = (float)ck;
     }
+}
+
+// y = a x + b for a double-float x = (xh, xl) and double-float constants a, b (an exact product of
+// the high parts by fma, the small cross terms added to its error): about 2^-46 relative, on the
+// FP32 pipe
+__device__ __forceinline__ void df_affine(float xh, float xl, float2 a, float2 b, float& yh, float& yl) {
+    const float p = __fmul_rn(a.x, xh);
+    const float t = fmaf(a.x, xl, fmaf(a.y, xh, fmaf(a.x, xh, -p)));
+    float s, e;
+    two_sum(p, b.x, s, e);
+    e = __fadd_rn(e, __fadd_rn(t, b.y));
+    fast_two_sum(s, e, yh, yl);
+}
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+// (xh + xl) < (t.x + t.y) for double-floats, exact in sign where the high parts are within a factor 2
+__device__ __forceinline__ bool df_less(float xh, float xl, float2 t) {
+    return __fadd_rn(__fsub_rn(xh, t.x), __fsub_rn(xl, t.y)) < 0.0f;
 }
 
 // double-float <-> FP64
@@ -457,18 +482,18 @@ __global__ void __launch_bounds__(128, 3) k_tm_step(TMConst C, MTracks M, uint32
                 if (p[2] > C.seam_mm) {
                     const int i = nearest_portf(C.G, p[0], p[1]);
                     if (hypf2(p[0] - C.mouth_mm[i][0], p[1] - C.mouth_mm[i][1]) < C.G.ap_r) {
-                        // enter (lib.rs:338-367) in FP64, then the port's grid units
+                        // enter (lib.rs:338-367): straight into the port's grid units
                         uint32_t* cnt = counts + (size_t)i * kNC;
-                        double x[3], v[3];
-                        for (int d = 0; d < 3; ++d) {
-                            x[d] = C.clo_m[d] + ddv(xh[d], xl[d]) * C.ch_m;
-                            v[d] = ddv(uh[d], ul[d]) * C.cu2v_d;
-                        }
-                        x[0] += C.axis_m - C.mouth_m[i][0];
-                        x[1] += C.axis_m - C.mouth_m[i][1];
-                        const double depth = x[2] - C.seam_m;
-                        if (reg == R_SPLIT) {
-                            x[2] = Z_RETURN + depth;
+                        const bool fwd = reg == R_SPLIT;
+                        const float2 a = C.en_a[i];
+                        df_affine(xh[0], xl[0], a, C.en_b[i][0], xh[0], xl[0]);
+                        df_affine(xh[1], xl[1], a, C.en_b[i][1], xh[1], xl[1]);
+                        df_affine(xh[2], xl[2], fwd ? a : neg2(a), C.en_b[i][fwd ? 2 : 3], xh[2], xl[2]);
+                        const float2 z0 = make_float2(0.0f, 0.0f);
+                        df_affine(uh[0], ul[0], a, z0, uh[0], ul[0]);
+                        df_affine(uh[1], ul[1], a, z0, uh[1], ul[1]);
+                        df_affine(uh[2], ul[2], fwd ? a : neg2(a), z0, uh[2], ul[2]);
+                        if (fwd) {
                             atomicAdd(cnt + 0, 1u);
                             if (last >= 0) {
                                 atomicAdd(cnt + 3, 1u);
@@ -476,16 +501,9 @@ __global__ void __launch_bounds__(128, 3) k_tm_step(TMConst C, MTracks M, uint32
                                 if (last != i) atomicAdd(cnt + 4, 1u);
                             }
                         } else {
-                            x[2] = Z_EXIT - depth;
-                            v[2] = -v[2];
                             atomicAdd(cnt + 14, 1u);
                         }
                         reg = 1 + i;
-                        const double ih = C.port[i].inv_hd, v2u = C.port[i].v2u_d;
-                        for (int d = 0; d < 3; ++d) {
-                            splitd(x[d] * ih, xh[d], xl[d]);
-                            splitd(v[d] * v2u, uh[d], ul[d]);
-                        }
                         region_consts(C, reg, qmdt2, rk);
                         cell_for(rk, reg, xh, c);
                         continue;
@@ -512,32 +530,27 @@ __global__ void __launch_bounds__(128, 3) k_tm_step(TMConst C, MTracks M, uint32
                 if (crash) {
                     reg = R_LOST;
                     atomicAdd(cnt + 15, 1u);
-                } else if (xh[2] < rk.zret || xh[2] > rk.zexit) {
-                    // leave (lib.rs:368-385) in FP64, then the cube's grid units
-                    const double h = C.port[i].h, u2v = C.port[i].u2v_d;
-                    double x[3], v[3];
-                    for (int d = 0; d < 3; ++d) {
-                        x[d] = ddv(xh[d], xl[d]) * h;
-                        v[d] = ddv(uh[d], ul[d]) * u2v;
-                    }
-                    x[0] += C.mouth_m[i][0] - C.axis_m;
-                    x[1] += C.mouth_m[i][1] - C.axis_m;
-                    if (x[2] < Z_RETURN) {
-                        x[2] = C.seam_m + x[2] - Z_RETURN;
+                } else if ((xh[2] < rk.zret + 1.0f && df_less(xh[2], xl[2], C.zr[i])) ||
+                           (xh[2] > rk.zexit - 1.0f && df_less(C.ze[i].x, C.ze[i].y, make_float2(xh[2], xl[2])))) {
+                    // leave (lib.rs:368-385) through the plane crossed, decided on the double-float z,
+                    // straight into the cube's grid units
+                    const bool ret = df_less(xh[2], xl[2], C.zr[i]);
+                    const float2 a = C.lv_a[i], z0 = make_float2(0.0f, 0.0f);
+                    df_affine(xh[0], xl[0], a, C.lv_b[i][0], xh[0], xl[0]);
+                    df_affine(xh[1], xl[1], a, C.lv_b[i][1], xh[1], xl[1]);
+                    df_affine(xh[2], xl[2], ret ? a : neg2(a), C.lv_b[i][ret ? 2 : 3], xh[2], xl[2]);
+                    df_affine(uh[0], ul[0], a, z0, uh[0], ul[0]);
+                    df_affine(uh[1], ul[1], a, z0, uh[1], ul[1]);
+                    df_affine(uh[2], ul[2], ret ? a : neg2(a), z0, uh[2], ul[2]);
+                    if (ret) {
                         reg = R_SPLIT;
                         last = i;
                         atomicAdd(cnt + 1, 1u);
                     } else {
-                        x[2] = C.seam_m - (x[2] - Z_EXIT);
-                        v[2] = -v[2];
                         reg = R_COMBINE;
                         last = -1;
                         atomicAdd(cnt + 2, 1u);
                         atomicAdd(cnt + 16 + sp, 1u);
-                    }
-                    for (int d = 0; d < 3; ++d) {
-                        splitd((x[d] - C.clo_m[d]) * C.inv_ch_m, xh[d], xl[d]);
-                        splitd(v[d] * C.cv2u_d, uh[d], ul[d]);
                     }
                     region_consts(C, reg, qmdt2, rk);
                     cell_for(rk, reg, xh, c);
@@ -690,6 +703,24 @@ State* create(const mq_tandem_desc& d, const DevFields& f, cudaStream_t st, std:
             C.mouth_m[i][k] = mouths[2 * i + k];
             C.mouth_mm[i][k] = (float)(mouths[2 * i + k] * 1000.0);
         }
+    // region-change maps (enter: lib.rs:338-367, leave: lib.rs:368-385) in grid coordinates
+    auto df = [](double v) { const float h = (float)v; return make_float2(h, (float)(v - (double)h)); };
+    for (int i = 0; i < 9; ++i) {
+        const double hp = d.port[i].h, hc = C.ch_m;
+        const double dx = C.axis_m - C.mouth_m[i][0], dy = C.axis_m - C.mouth_m[i][1];
+        C.en_a[i] = df(hc / hp);
+        C.en_b[i][0] = df((C.clo_m[0] + dx) / hp);
+        C.en_b[i][1] = df((C.clo_m[1] + dy) / hp);
+        C.en_b[i][2] = df((Z_RETURN + C.clo_m[2] - C.seam_m) / hp);   // from the splitter
+        C.en_b[i][3] = df((Z_EXIT - C.clo_m[2] + C.seam_m) / hp);     // from the combiner, z reversed
+        C.lv_a[i] = df(hp / hc);
+        C.lv_b[i][0] = df((-dx - C.clo_m[0]) / hc);
+        C.lv_b[i][1] = df((-dy - C.clo_m[1]) / hc);
+        C.lv_b[i][2] = df((C.seam_m - Z_RETURN - C.clo_m[2]) / hc);    // back to the splitter
+        C.lv_b[i][3] = df((C.seam_m + Z_EXIT - C.clo_m[2]) / hc);      // on to the combiner, z reversed
+        C.zr[i] = df(Z_RETURN / hp);
+        C.ze[i] = df(Z_EXIT / hp);
+    }
     // ports: one packed record array per distinct (grid arrays, idle)
     struct Key { const float4 *rf, *ac, *dc, *gate; int idle; const float4* rec; };
     std::vector<Key> made;
