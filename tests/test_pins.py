@@ -67,7 +67,7 @@ def test_grid_study_counts_within_binomial():
     assert o["transmitted"] == g["transmit"] == 0
     assert o["timeout"] == g["timeout"] == 0
     for ours, theirs in ((o["returned"], g["returned"]), (o["crashed"], g["electrode"]), (o["left"], g["box"])):
-        assert abs(pull(ours, n, theirs, n)) <= 2.5, (ours, theirs)
+        assert abs(pull(ours, n, theirs, n)) <= 2.0, (ours, theirs)   # the reference's own rule
 
 
 def test_s14_counts_within_reference_pull_rule():
