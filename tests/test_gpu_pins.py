@@ -4,9 +4,8 @@ channel and drive): the FP64 kernel reproduces the oracle's committed counts exa
 bit-exact with the oracle on the same grid, and the grid solved on the GPU is bit-identical to the
 host's); both engines meet the reference's own bar against chsim's counts (|pull| <= 2 on its rows
 T, C, R and T/(T+C), validate.rs:119-135), and the mixed engine, an independent random stream,
-agrees with the FP64 kernel within 3 sigma on every count."""
+agrees with the FP64 kernel at the 95% level (one chi-square over the four outcome classes)."""
 import json
-import math
 from pathlib import Path
 
 import pytest
@@ -14,11 +13,6 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 PINS = json.loads((Path(__file__).parent / "golden" / "pins.json").read_text())
-
-
-def _pull(k1, n1, k2, n2):
-    p1, p2 = k1 / n1, k2 / n2
-    return (p1 - p2) / max(math.sqrt(p1 * (1 - p1) / n1 + p2 * (1 - p2) / n2), 1e-12)
 
 
 def _as_rows(c):
@@ -41,8 +35,8 @@ def test_s14_point_on_the_device(built):
     for c in (c64, cm):
         for row in V.rows(c, metal):
             assert abs(row.pull()) <= 2.0, (row.name, row.live, row.refv, row.pull())
-    # the mixed engine (an independent random stream) against the FP64 kernel, timeouts included
-    for row in V.rows(cm, c64):
-        assert abs(row.pull()) <= 3.0, (row.name, row.pull())
-    n = s["n"]
-    assert abs(_pull(cm.timeout, n, c64.timeout, n)) <= 3.0
+    # the mixed engine (an independent random stream) against the FP64 kernel at the 95% level: one
+    # chi-square over the four classes (transmitted, crashed or left, returned, timeout), p >= 0.05
+    r = V.compare_classes({"t": cm.trans, "c": cm.crash, "r": cm.ret, "to": cm.timeout},
+                          {"t": c64.trans, "c": c64.crash, "r": c64.ret, "to": c64.timeout})
+    assert r["p"] >= 0.05, r
