@@ -110,12 +110,15 @@ def grid_workload(ions_per_job: int = 1000, njobs: int = 1024):
 
 
 def apply_tuning(eng, args) -> None:
-    """Launch-shape overrides from the command line (--chunk, --sort-cells, --no-graph)."""
+    """Launch-shape overrides from the command line (--chunk, --sort-cells, --no-graph,
+    --blocks-per-sm)."""
     kw = {}
     if args.chunk:
         kw["chunk"] = args.chunk
     if args.sort_cells:
         kw["sort_cells"] = True
+    if args.blocks_per_sm:
+        kw["blocks_per_sm"] = args.blocks_per_sm
     if args.no_graph:
         kw["use_graph"] = False
     if kw:
@@ -193,6 +196,8 @@ def run_gridstudy(args, rank: int, world: int):
                                 "roofline_l2_frac": (moved / (step_ms * 1e-3) / 1e9 / l2) if l2 else None},
                       "fp64_gpu": {"value": s64.ion_steps / (s64.kernel_ms * 1e-3), "unit": UNIT} if s64 else None,
                       "counts": pulls,
+                      "mixed_counts": {k: int(sum(getattr(o, k) for o in om))
+                                       for k in ("crashed", "returned", "transmitted", "left", "timeout")},
                       "class_agreement": agree})
         value = rate
         del f
@@ -706,6 +711,7 @@ def main():
     ap.add_argument("--chunk", type=int, default=0, help="steps per launch of the mixed engine (0 = its tuning)")
     ap.add_argument("--sort-cells", action="store_true", help="Morton cell order of every launch's live list")
     ap.add_argument("--no-graph", action="store_true", help="issue a multi-launch sequence without a CUDA graph")
+    ap.add_argument("--blocks-per-sm", type=int, default=0, help="resident blocks per SM of the mixed engine (0 = tuning)")
     ap.add_argument("--grid", type=float, default=0.0, help="gridstudy: only the grid of this spacing [mm]")
     ap.add_argument("--replicas", type=int, default=16, help="legacy: seed sets of the 26 x 1,000-ion scan")
     ap.add_argument("--sweep-only", action="store_true",
