@@ -145,6 +145,7 @@ def run_gridstudy(args, rank: int, world: int):
     grids = []
     clocks = Clocks(local)
     value = None
+    cpu, fin_f = None, None
     spacings = [h for h in GRID_SPACINGS if not args.grid or abs(h - args.grid) < 1e-4]
     for h in spacings:
         t0 = time.perf_counter()
@@ -159,6 +160,7 @@ def run_gridstudy(args, rank: int, world: int):
                 clocks.start()
             ms, steps = [], 0
             walls = []
+            launches = 0
             for _ in range(args.steps):
                 flush_l2(flush)
                 torch.cuda.synchronize()
@@ -167,6 +169,7 @@ def run_gridstudy(args, rank: int, world: int):
                 walls.append(time.perf_counter() - w0)
                 ms.append(eng.last_stats.kernel_ms)
                 steps = eng.last_stats.ion_steps
+                launches += eng.last_stats.kernel_launches
             step_ms = eng.last_stats.step_kernel_ms
             moved = stepping_bytes(eng.last_stats, tuned["wide_records"])
             loads_per_step = eng.last_stats.cell_loads / max(steps, 1)
@@ -188,7 +191,7 @@ def run_gridstudy(args, rank: int, world: int):
         grids.append({"h_mm": h, "dims": [f.nx, f.ny, f.nz], "nodes": nodes,
                       "node_records_gb": nodes * (64 if tuned["wide_records"] else 48) / 1e9, "solve_s": t_solve,
                       "tuning": tuned,
-                      "mixed": {"value": rate, "unit": UNIT, "ms_per_step": float(np.mean(ms)),
+                      "mixed": {"value": rate, "unit": UNIT, "ms_per_step": float(np.mean(ms)), "gpu_launches": int(launches),
                                 "e2e": steps / float(np.mean(walls)), "ion_steps": int(steps),
                                 "cell_loads_per_ion_step": loads_per_step,
                                 "achieved_gbs": moved / (step_ms * 1e-3) / 1e9,
@@ -200,8 +203,17 @@ def run_gridstudy(args, rank: int, world: int):
                                        for k in ("crashed", "returned", "transmitted", "left", "timeout")},
                       "class_agreement": agree})
         value = rate
+        fin_f = f if h == spacings[-1] else None
         del f
     clk = clocks.stop()
+    if fin_f is not None and not args.no_cpu and rank == 0:
+        # the C oracle on the host cores, on the grid the line's value is quoted for (after the
+        # clock sampling: the GPU idles meanwhile)
+        r = cpu_rate(jobs, ph, dc, fin_f, 8, os.cpu_count() or 1, target_s=10.0)
+        cpu = {"value": r["value"], "unit": UNIT, "cores": os.cpu_count() or 1, "cpu": cpu_model(), "kind": "port",
+               "grid_mm": spacings[-1],
+               "sample": f"{r['ions']} ions of {r['jobs']} evenly spaced jobs run to completion ({r['seconds']:.1f} s)"}
+    del fin_f
     if rank != 0:
         return
     fin = grids[-1]
@@ -213,7 +225,7 @@ def run_gridstudy(args, rank: int, world: int):
                                    "0.0333 mm grid", "l2_flush": "256 MB write before every timed step"},
             "e2e": {"value": fin["mixed"]["e2e"], "unit": UNIT, "h2d_bytes_per_step": int(table.arr.nbytes),
                     "d2h_bytes_per_step": int(len(jobs) * 64)},
-            "gpu_launches": None,
+            "gpu_launches": fin["mixed"]["gpu_launches"],
             "roofline": {"bound": "hbm", "achieved": fin["mixed"]["achieved_gbs"], "peak": hbm, "unit": "GB/s",
                          "frac": fin["mixed"]["roofline_frac"], "traffic": None,
                          "peak_source": "measured hbm_gbs" if peaks.get("hbm_gbs") else "fallback",
@@ -224,7 +236,7 @@ def run_gridstudy(args, rank: int, world: int):
             "roofline_l2": {"achieved": fin["mixed"]["achieved_gbs"], "peak": l2, "unit": "GB/s",
                             "frac": fin["mixed"]["roofline_l2_frac"],
                             "peak_source": "L2 read bandwidth measured in this run (mq_measure_l2_read_gbs)"},
-            "cpu_baseline": None, "clocks": clk, "grids": grids}
+            "cpu_baseline": cpu, "clocks": clk, "grids": grids}
     return line
 
 
