@@ -17,10 +17,13 @@
 //   * RF / AC phase as exact 64-bit fixed-point turn accumulators (phase = offset +
 //     step * f * dt mod 1), evaluated with an FP32 quarter-turn polynomial;
 //   * Philox-4x32-10 counter RNG keyed by the ion's 64-bit key, counter = step (thermal candidates
-//     and collisions) or 4-step window (legacy collisions: two blocks per window);
+//     and collisions) or 4-step window (legacy collisions: two blocks per window); thermal
+//     candidates drawn against the majorant |v| + E|V| (mqx::thermal_partner), which samples the
+//     reference's collision process with 2-4 times fewer candidates than its |v| + 6 s_gas;
 //   * device injection with the FP64 injection's draws and FP32 transforms (k_inject_mixed).
 #include "mq_mixed.h"
 #include "mq_check.h"
+#include "mq_mixmath.h"
 
 #include <cstring>
 #include <vector>
@@ -30,6 +33,7 @@ namespace {
 
 using mqd::DevGrid;
 using mqd::DevIons;
+using namespace mqx;
 
 constexpr unsigned FULL = 0xffffffffu;
 
@@ -41,26 +45,6 @@ struct Ctrs {                       // device counters (40 B)
     unsigned long long cell_loads;  // cell-cache fills (8 node records each)
     unsigned long long queued;      // ions queued over the call's launches
 };
-
-// ---------------------------------------------------------------- Philox-4x32-10
-// Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy as 1, 2, 3" (SC'11).
-__device__ __forceinline__ uint4 philox(uint32_t k0, uint32_t k1, uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3) {
-#pragma unroll
-    for (int r = 0; r < 10; ++r) {
-        if (r) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
-        uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
-        uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
-        uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
-        c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
-    }
-    return make_uint4(c0, c1, c2, c3);
-}
-__device__ __forceinline__ float unif(uint32_t x) { return (float)(x >> 8) * 0x1.0p-24f; }   // top 24 bits
-__device__ __forceinline__ float unif16(uint32_t x16) { return (float)x16 * 0x1.0p-16f; }      // a 16-bit field
-// sin / cos of a uniform angle 2 pi u - pi (u in [0, 1)): the hardware approximations are accurate to
-// about 2^-21 on [-pi, pi], far below the Monte Carlo noise of the draws they serve, and a uniform
-// angle shifted by pi is still uniform
-__device__ __forceinline__ void angle_sincos(float u, float* s, float* c) { __sincosf(fmaf(u, 6.28318531f, -3.14159265f), s, c); }
 
 // ---------------------------------------------------------------- FP32 turn-based sine
 // sin / cos Taylor polynomials on [-pi/4, pi/4] (coefficients (-1)^k/(2k+1)!, (-1)^k/(2k)!)
@@ -95,17 +79,6 @@ __device__ __forceinline__ void rotate(float& s, float& c, float cw, float sw) {
     s = s2;
 }
 
-// ---------------------------------------------------------------- double-float helpers
-__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
-    s = __fadd_rn(a, b);
-    float bb = __fsub_rn(s, a);
-    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
-}
-__device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& e) {
-    s = __fadd_rn(a, b);
-    e = __fsub_rn(b, __fsub_rn(s, a));
-}
-
 // ---------------------------------------------------------------- cell cache
 // Interleaved node records: node q occupies float4 [Sq] = {RF.xyz, conductor mask},
 // [Sq+1] = {combined DC.xyz, conductor bits of the cell based at q}, [Sq+2] = {AC.xyz, 0}, with
@@ -127,11 +100,6 @@ __device__ __forceinline__ uint32_t node_of(const MixBatch& B, int32_t ci, int32
     return (uint32_t)ci + (uint32_t)B.nx * ((uint32_t)cj + (uint32_t)B.ny * (uint32_t)ck);
 }
 
-// 32 bytes from a 32-byte aligned address (ld.global.nc.v8.f32, sm_100 and later): two float4
-__device__ __forceinline__ void ld256(const float4* p, float4& a, float4& b) {
-    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w) : "l"(p));
-}
 // the same without allocating the lines in L1 (they are fetched from L2 into registers)
 __device__ __forceinline__ void ld256_na(const float4* p, float4& a, float4& b) {
     asm("ld.global.nc.L1::no_allocate.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
@@ -200,8 +168,6 @@ __device__ __forceinline__ float field_comp(const float R[8], const float D[8], 
     const float c0 = fmaf(ty, c10 - c00, c00), c1 = fmaf(ty, c11 - c01, c01);
     return fmaf(tz, c1 - c0, c0);
 }
-
-__device__ __forceinline__ int32_t clampi(int32_t v, int32_t lo, int32_t hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
 // (xh + xl) - (th + tl) for a double-float position and threshold, as the sign-exact difference of
 // two double-floats: xh - th is exact wherever the two are within a factor of 2 of each other (which
@@ -385,33 +351,26 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
             // ---- collisions
             if (!LEGACY) {
                 const float u0 = unif((nprev & 3) == 0 ? rc.x : (nprev & 3) == 1 ? rc.y : (nprev & 3) == 2 ? rc.z : rc.w);
-                // candidate if u0 < cand_a |u| + cand_b, tested on squares (no square root per step)
+                // candidate if u0 < cand_a |u| + cand_b = n sigma dt (|v| + E|V|), tested on squares
+                // (no square root per step); see thermal_partner for why E|V| bounds the rate
                 const float um2 = fmaf(uh[0], uh[0], fmaf(uh[1], uh[1], uh[2] * uh[2]));
                 const float du = u0 - cand_b;
                 if (du < 0.0f || du * du < cand_a * cand_a * um2) {
                     const float um = sqrtf(um2);
                     const float s_gas = sj_sgas[threadIdx.x], mr = sj_mr[threadIdx.x];
-                    // one Philox block (128 bits) per candidate: two 24-bit uniforms for the
-                    // Box-Muller radii, and five 16-bit uniforms (two Box-Muller angles, the
-                    // acceptance draw, cos(theta) and phi of the scattering direction)
+                    // two Philox blocks per candidate, drawn side by side: the first for the gas
+                    // partner and the acceptance, the second for the scattering direction
                     const uint4 r0 = philox(k0, k1, nprev, 1u, 0u, 0u);
+                    const uint4 r1 = philox(k0, k1, nprev, 2u, 0u, 0u);
                     const float u2v = B.u2v_f;
                     float v[3] = {uh[0] * u2v, uh[1] * u2v, uh[2] * u2v};
-                    const float bound = fmaf(um, u2v, 6.0f * s_gas);
-                    const float g1 = sqrtf(-2.0f * __logf(fmaxf(unif(r0.x), 0x1.0p-25f)));
-                    const float g2 = sqrtf(-2.0f * __logf(fmaxf(unif(r0.y), 0x1.0p-25f)));
-                    float s1, c1, s2, c2;
-                    angle_sincos(unif16(r0.z >> 16), &s1, &c1);
-                    angle_sincos(unif16(r0.z & 0xffffu), &s2, &c2);
-                    float gv[3];
-                    gv[0] = fmaf(-s_gas, g1 * c1, v[0]);
-                    gv[1] = fmaf(-s_gas, g1 * s1, v[1]);
-                    gv[2] = fmaf(-s_gas, g2 * c2, v[2]);
+                    float gv[3], vm_sum;
+                    thermal_partner(r0, s_gas, um * u2v, v, gv, vm_sum);
                     const float gl = sqrtf(fmaf(gv[0], gv[0], fmaf(gv[1], gv[1], gv[2] * gv[2])));
-                    if (unif16(r0.w >> 16) * bound < gl) {
-                        const float cth = 2.0f * unif16(r0.w & 0xffffu) - 1.0f;
+                    if (unif16(r0.w & 0xffffu) * vm_sum < gl) {
+                        const float cth = 2.0f * unif(r1.x) - 1.0f;
                         float sp, cp;
-                        angle_sincos(unif16(((r0.x & 0xffu) << 8) | (r0.y & 0xffu)), &sp, &cp);
+                        angle_sincos(unif(r1.y), &sp, &cp);
                         const float sn = sqrtf(fmaxf(0.0f, 1.0f - cth * cth));
                         const float nn[3] = {sn * cp, sn * sp, cth};
                         const float v2u = B.v2u_f;
@@ -812,7 +771,7 @@ MixJob make_mix_job(const mqp::JobC& j, const mqp::Batch& b) {
     m.kick = (float)(j.qmdt * b.dt / b.h);
     m.v_ac = (float)j.v_ac;
     m.cand_a = (float)(j.nsd * b.h / b.dt);
-    m.cand_b = (float)(j.nsd * 6.0 * j.s_gas);
+    m.cand_b = (float)(j.nsd * 1.5957691216057308 * j.s_gas);   // n sigma dt E|V| (thermal_partner)
     m.s_gas = (float)j.s_gas;
     m.mr = (float)j.mr;
     m.floor_v = (float)j.floor_v;

@@ -18,7 +18,9 @@
 //     registers and reloaded on a cell change;
 //   * drive values per global step from the FP64 engine's drive table, rounded to FP32; thermal
 //     collisions with Philox-4x32-10 keyed by the track key and the global step (all lanes
-//     share the global step, so the generator runs warp-uniformly);
+//     share the global step, so the generator runs warp-uniformly), their candidates drawn
+//     against the majorant |v| + E|V| of mqx::thermal_partner (the reference's |v| + 6 s_gas
+//     samples the same process with 2-4 times as many candidates);
 //   * cube losses by the geometry test in FP32, skipped in the interior box where every
 //     face is farther than the post tops (geometry.rs:166 makes such points free).
 #include <cmath>
@@ -29,9 +31,12 @@
 #include "mq_phys.h"
 #include "mq_tandem_internal.h"
 #include "mq_check.h"
+#include "mq_mixmath.h"
 
 namespace mqtm {
 namespace {
+
+using namespace mqx;
 
 constexpr unsigned FULL = 0xffffffffu;
 constexpr int R_SPLIT = 0, R_COMBINE = 10, R_LOST = 11;
@@ -39,33 +44,6 @@ constexpr int kNC = 21;        // counters per port
 constexpr int kBuckets = 11;   // live regions 0..10
 constexpr double Z_EXIT = 18.6e-3, Z_RETURN = 0.5e-3;   // world.rs:21-22
 constexpr uint32_t kChunk = 256;                        // global steps per launch
-
-// ---------------------------------------------------------------- Philox-4x32-10
-// Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy as 1, 2, 3" (SC'11).
-__device__ __forceinline__ uint4 philox(uint32_t k0, uint32_t k1, uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3) {
-#pragma unroll
-    for (int r = 0; r < 10; ++r) {
-        if (r) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
-        const uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
-        const uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
-        const uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
-        c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
-    }
-    return make_uint4(c0, c1, c2, c3);
-}
-__device__ __forceinline__ float unif(uint32_t x) { return (float)(x >> 8) * 0x1.0p-24f; }
-__device__ __forceinline__ float unif16(uint32_t x16) { return (float)x16 * 0x1.0p-16f; }
-__device__ __forceinline__ void angle_sincos(float u, float* s, float* c) { __sincosf(fmaf(u, 6.28318531f, -3.14159265f), s, c); }
-
-__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
-    s = __fadd_rn(a, b);
-    const float bb = __fsub_rn(s, a);
-    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
-}
-__device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& e) {
-    s = __fadd_rn(a, b);
-    e = __fsub_rn(b, __fsub_rn(s, a));
-}
 
 // ---------------------------------------------------------------- constants
 struct CubeF {   // cube geometry in mm, growth 0 (geometry.rs:136-205)
@@ -182,7 +160,6 @@ __device__ __forceinline__ float lerp3(const float F[8], float tx, float ty, flo
     return fmaf(tz, c1 - c0, c0);
 }
 
-__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
 // Register cache of the track's cell: the 8 corners x {RF, DC, AC} of its region's grid,
 // reloaded only when the track changes cell or region (cube cells leave A unused).
@@ -226,11 +203,6 @@ __device__ __forceinline__ void region_consts(const TMConst& C, int reg, float q
     }
 }
 
-// 32 bytes from a 32-byte aligned address (ld.global.nc.v8.f32, sm_100 and later): two float4
-__device__ __forceinline__ void ld256(const float4* p, float4& a, float4& b) {
-    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w) : "l"(p));
-}
 
 // the cell of grid position x (clamped to the grid), reloading the cache when it changes; a change
 // is found on floored floats, and indices are formed only when one is seen
@@ -437,28 +409,24 @@ __global__ void __launch_bounds__(128, 3) k_tm_step(TMConst C, MTracks M, uint32
                 e = __fadd_rn(e, __fadd_rn(xl[d], ul[d]));
                 fast_two_sum(s, e, xh[d], xl[d]);
             }
-            // null-collision thermal bath (world.rs:473-488): candidate if u0 < nsd (|v| + 6 s_gas)
+            // null-collision thermal bath (world.rs:473-488) with the majorant |v| + E|V| of
+            // thermal_partner: candidate if u0 < nsd (|v| + E|V|)
             {
                 const uint32_t q = (uint32_t)(g & 3);
                 const float u0 = unif(q == 0 ? rc.x : q == 1 ? rc.y : q == 2 ? rc.z : rc.w);
                 const float um2 = fmaf(uh[0], uh[0], fmaf(uh[1], uh[1], uh[2] * uh[2]));
-                const float ca = nsd * u2v, du = u0 - nsd * 6.0f * C.s_gas;
+                const float ca = nsd * u2v, du = u0 - nsd * kMeanSpeed * C.s_gas;
                 if (du < 0.0f || du * du < ca * ca * um2) {
                     const uint4 r0 = philox(k0, k1, (uint32_t)g, (uint32_t)(g >> 32), 1u, 0u);
+                    const uint4 r1 = philox(k0, k1, (uint32_t)g, (uint32_t)(g >> 32), 2u, 0u);
                     const float v[3] = {uh[0] * u2v, uh[1] * u2v, uh[2] * u2v};
-                    const float bound = fmaf(sqrtf(um2), u2v, 6.0f * C.s_gas);
-                    const float g1 = sqrtf(-2.0f * __logf(fmaxf(unif(r0.x), 0x1.0p-25f)));
-                    const float g2 = sqrtf(-2.0f * __logf(fmaxf(unif(r0.y), 0x1.0p-25f)));
-                    float s1, c1, s2, c2;
-                    angle_sincos(unif16(r0.z >> 16), &s1, &c1);
-                    angle_sincos(unif16(r0.z & 0xffffu), &s2, &c2);
-                    const float gv[3] = {fmaf(-C.s_gas, g1 * c1, v[0]), fmaf(-C.s_gas, g1 * s1, v[1]),
-                                         fmaf(-C.s_gas, g2 * c2, v[2])};
+                    float gv[3], vm_sum;
+                    thermal_partner(r0, C.s_gas, sqrtf(um2) * u2v, v, gv, vm_sum);
                     const float gl = sqrtf(fmaf(gv[0], gv[0], fmaf(gv[1], gv[1], gv[2] * gv[2])));
-                    if (unif16(r0.w >> 16) * bound < gl) {
-                        const float cth = 2.0f * unif16(r0.w & 0xffffu) - 1.0f;
+                    if (unif16(r0.w & 0xffffu) * vm_sum < gl) {
+                        const float cth = 2.0f * unif(r1.x) - 1.0f;
                         float sp_, cp_;
-                        angle_sincos(unif16(((r0.x & 0xffu) << 8) | (r0.y & 0xffu)), &sp_, &cp_);
+                        angle_sincos(unif(r1.y), &sp_, &cp_);
                         const float sn = sqrtf(fmaxf(0.0f, 1.0f - cth * cth));
                         const float nn[3] = {sn * cp_, sn * sp_, cth};
                         const float v2u = 1.0f / u2v;

@@ -39,4 +39,9 @@ def test_s14_point_on_the_device(built):
     # chi-square over the four classes (transmitted, crashed or left, returned, timeout), p >= 0.05
     r = V.compare_classes({"t": cm.trans, "c": cm.crash, "r": cm.ret, "to": cm.timeout},
                           {"t": c64.trans, "c": c64.crash, "r": c64.ret, "to": c64.timeout})
+    print(f"PARITY S14 point: FP64 T {c64.trans} C+L {c64.crash} R {c64.ret} TO {c64.timeout}; mixed T {cm.trans} "
+          f"C+L {cm.crash} R {cm.ret} TO {cm.timeout}; mixed vs FP64 chi2 {r['chi2']:.2f} dof {r['dof']} p {r['p']:.3f}; "
+          "pulls vs chsim (T, C, R, T/(T+C)): FP64 "
+          + " ".join(f"{row.pull():+.2f}" for row in V.rows(c64, metal)) + ", mixed "
+          + " ".join(f"{row.pull():+.2f}" for row in V.rows(cm, metal)))
     assert r["p"] >= 0.05, r
