@@ -16,12 +16,10 @@
 //     crash test), with an optional L1 prefetch of the cell the ion is heading for;
 //   * RF / AC phase as exact 64-bit fixed-point turn accumulators (phase = offset +
 //     step * f * dt mod 1), evaluated with an FP32 quarter-turn polynomial;
-//   * Philox-4x32-10 counter RNG keyed by the ion's 64-bit key, counter = step (thermal collision
-//     candidates) or 4-step window (legacy collisions: two blocks per window); thermal candidates
-//     drawn against the majorant |v| + E|V| (mqx::thermal_partner), which samples the reference's
-//     collision process with 2-4 times fewer candidates than its |v| + 6 s_gas, and found by the
-//     ion's optical depth (an Exp(1) draw per candidate, spent at -ln(1 - p) per step) instead of a
-//     uniform per step;
+//   * Philox-4x32-10 counter RNG keyed by the ion's 64-bit key, counter = step (thermal candidates
+//     and collisions) or 4-step window (legacy collisions: two blocks per window); thermal
+//     candidates drawn against the majorant |v| + E|V| (mqx::thermal_partner), which samples the
+//     reference's collision process with 2-4 times fewer candidates than its |v| + 6 s_gas;
 //   * device injection with the FP64 injection's draws and FP32 transforms (k_inject_mixed).
 #include "mq_mixed.h"
 #include "mq_check.h"
@@ -187,8 +185,7 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
         float* __restrict__ keep, const uint64_t* __restrict__ kph, uint32_t n_all) {
     // keep: the working state of every ion of the call in grid units, double-float position and
     // velocity (12 floats per ion, structure of arrays over n_all), filled from the FP64 states by
-    // k_init_list and written back to them by k_unstage, so this kernel does no FP64 arithmetic,
-    // then the thermal-gas optical depth (a 13th array, carried across the call's launches);
+    // k_init_list and written back to them by k_unstage, so this kernel does no FP64 arithmetic;
     // kph: the RF / AC phase offsets as 64-bit fixed-point turns (two arrays of n_all)
     // The job constants only the collision branches read are staged per lane in shared memory at
     // refill, so those divergent branches do not wait on a global load (1.5% on the sweep, 5% on the
@@ -210,11 +207,10 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
     float srf = 0.f, crf = 1.f, sac = 0.f, cac = 1.f, cw_ac = 1.f, sw_ac = 0.f;
     float kick = 0.f, v_ac = 0.f, cand_a = 0.f, cand_b = 0.f;
     uint32_t k0 = 0, k1 = 0;
-    // legacy collisions: the Philox blocks of the current 4-step window (rc, rn), drawn for every lane
-    // on a warp-uniform schedule (every 4 loop iterations), so the 10-round generator runs with all
-    // lanes active; thermal gas: the optical depth left to the next collision candidate
+    // per-step candidate uniforms: Philox block n>>2 (rc) and the next block (rn); rn is
+    // refreshed for every lane on a warp-uniform schedule (every 4 loop iterations), so the
+    // 10-round generator runs with all lanes active instead of once per lane-boundary
     uint4 rc = make_uint4(0, 0, 0, 0), rn = make_uint4(0, 0, 0, 0);
-    float tau = 0.f;
     uint32_t iter = 0;
     uint32_t loads = 0;                 // cell-cache fills of this lane
     Cell c;
@@ -285,7 +281,8 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
                     const uint64_t key = io.rng[id];
                     k0 = (uint32_t)key; k1 = (uint32_t)(key >> 32);
                     if (!LEGACY) {
-                        tau = keep[(size_t)12 * n_all + id];
+                        rc = philox(k0, k1, n >> 2, 0u, 0u, 0u);
+                        if (r4) rn = philox(k0, k1, (n >> 2) + 1u, 0u, 0u, 0u);
                     } else if (r4) {   // the legacy collision words of the current 4-step window
                         rc = philox(k0, k1, n >> 2, 2u, 0u, 0u);
                         rn = philox(k0, k1, n >> 2, 3u, 0u, 0u);
@@ -309,6 +306,7 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
         // then falls on the same steps of every ion, whatever the scheduling, so per-ion
         // results are reproducible bit for bit.
         const bool act = have && (((iter ^ n) & 3u) == 0u);
+        if (!LEGACY && (iter & 3u) == 0u && act) rn = philox(k0, k1, (n >> 2) + 1u, 0u, 0u, 0u);
         // legacy collisions draw from two Philox blocks per 4-step window, computed here with every
         // lane of the warp active (7% on the legacy scan against one block per collision inside
         // the divergent collision branch); a collision at window step q takes words 2q and 2q + 1
@@ -352,15 +350,13 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
             done += 1;
             // ---- collisions
             if (!LEGACY) {
-                // a step is a candidate with probability p = cand_a |u| + cand_b = n sigma dt (|v| + E|V|)
-                // (thermal_partner shows why E|V| bounds the rate): the ion's optical depth tau, an
-                // Exp(1) draw, loses -ln(1 - p) per step and a candidate comes when it runs out, which
-                // is the per-step Bernoulli(p) process itself, with no uniform drawn per step
+                const float u0 = unif((nprev & 3) == 0 ? rc.x : (nprev & 3) == 1 ? rc.y : (nprev & 3) == 2 ? rc.z : rc.w);
+                // candidate if u0 < cand_a |u| + cand_b = n sigma dt (|v| + E|V|), tested on squares
+                // (no square root per step); see thermal_partner for why E|V| bounds the rate
                 const float um2 = fmaf(uh[0], uh[0], fmaf(uh[1], uh[1], uh[2] * uh[2]));
-                const float um = sqrtf(um2);
-                const float p = fmaf(cand_a, um, cand_b);
-                tau -= p * fmaf(p, fmaf(p, 0.333333333f, 0.5f), 1.0f);   // -ln(1 - p) to p^4 / 4
-                if (tau < 0.0f) {
+                const float du = u0 - cand_b;
+                if (du < 0.0f || du * du < cand_a * cand_a * um2) {
+                    const float um = sqrtf(um2);
                     const float s_gas = sj_sgas[threadIdx.x], mr = sj_mr[threadIdx.x];
                     // two Philox blocks per candidate, drawn side by side: the first for the gas
                     // partner and the acceptance, the second for the scattering direction
@@ -385,8 +381,8 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
                         }
                         ncoll += 1;
                     }
-                    tau = -__logf(fmaxf(unif(r1.z), 0x1.0p-25f));   // the next candidate's optical depth
                 }
+                if ((n & 3) == 0) rc = rn;   // rn holds block n>>2: refreshed at most 3 iterations ago
             } else {
                 leg -= 1;
                 if (leg <= 0) {
@@ -470,7 +466,6 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
                     keep[(size_t)(0 + d) * n_all + id] = xh[d]; keep[(size_t)(3 + d) * n_all + id] = xl[d];
                     keep[(size_t)(6 + d) * n_all + id] = uh[d]; keep[(size_t)(9 + d) * n_all + id] = ul[d];
                 }
-                if (!LEGACY) keep[(size_t)12 * n_all + id] = tau;
                 steps_total += done;
                 append = status == 0;
                 have = false;
@@ -622,14 +617,6 @@ __global__ void k_init_list(DevIons io, uint32_t n, uint32_t* list, Ctrs* ctr, M
         }
         kph[i] = (uint64_t)(io.ph_rf[i] * 0x1.0p63) << 1;
         kph[(size_t)n + i] = (uint64_t)(io.ph_ac[i] * 0x1.0p63) << 1;
-        if (!B.legacy_coll) {
-            // thermal gas: the optical depth to the ion's first collision candidate of this call, an
-            // Exp(1) draw keyed by the ion and its step count (the depth is memoryless, so drawing it
-            // afresh where a call starts leaves the collision process unchanged)
-            const uint64_t key = io.rng[i];
-            const uint4 r = philox((uint32_t)key, (uint32_t)(key >> 32), io.steps[i], 3u, 0u, 0u);
-            keep[(size_t)12 * n + i] = -__logf(fmaxf(unif(r.x), 0x1.0p-25f));
-        }
     }
     const unsigned m = __ballot_sync(FULL, live);
     const uint32_t lane = threadIdx.x & 31;
@@ -989,9 +976,9 @@ cudaError_t run(Scratch& s, const Tuning& t, DevGrid g, uint64_t grid_gen, const
     const uint32_t full = (uint32_t)((need + chunk - 1) / chunk);
     const uint32_t launches = (t.max_launches && t.max_launches < full) ? t.max_launches : full;
     const uint32_t last_chunk = launches < full ? chunk : (uint32_t)(need - (uint64_t)(launches - 1) * chunk);
-    // working state: phase offsets (2 x u64), position / velocity double-floats (12 x f32), the
-    // optical depth of thermal gas (f32) and the staged flag (u8) of every ion
-    const size_t keep_bytes = (size_t)n * (2 * sizeof(uint64_t) + 13 * sizeof(float) + 1);
+    // working state: phase offsets (2 x u64), position / velocity double-floats (12 x f32) and the
+    // staged flag (u8) of every ion
+    const size_t keep_bytes = (size_t)n * (2 * sizeof(uint64_t) + 12 * sizeof(float) + 1);
     if (s.keep_cap < keep_bytes) {
         if (s.keep) cudaFree(s.keep);
         s.keep = nullptr; s.keep_cap = 0;
@@ -1008,7 +995,7 @@ cudaError_t run(Scratch& s, const Tuning& t, DevGrid g, uint64_t grid_gen, const
     if ((e = cudaMemsetAsync(ctr, 0, sizeof(Ctrs), st)) != cudaSuccess) return e;
     uint64_t* kph = static_cast<uint64_t*>(s.keep);
     float* keep = reinterpret_cast<float*>(kph + (size_t)2 * n);
-    uint8_t* staged = reinterpret_cast<uint8_t*>(keep + (size_t)13 * n);
+    uint8_t* staged = reinterpret_cast<uint8_t*>(keep + (size_t)12 * n);
     k_init_list<<<(n + 255) / 256, 256, 0, st>>>(io, n, static_cast<uint32_t*>(s.lists), ctr, mb, keep, kph, staged);
     info->kernel_launches += 1;
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
