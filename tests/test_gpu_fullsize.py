@@ -5,7 +5,8 @@
   grid): every ion finishes and is counted once; a rerun gives the same bits; every ion of
   sampled jobs has the state it gets when its job runs alone; on 16 ions of every job the mixed
   engine's outcome-class counts match the FP64 kernel's (which is bit-exact with the oracle) at the
-  95% level (one chi-square over the classes, p >= 0.05);
+  95% level (one chi-square over the classes, p >= 0.05), and so do the whole batch's totals over
+  four seed sets;
 * the tandem (1,048,576 tracks, nine 0.050 mm port grids): the region census conserves tracks
   at every frame, the port counters balance, and a rerun gives the same bits;
 * the default launch shapes of the finer grids.
@@ -18,7 +19,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def _sweep_jobs(mq, ions_per_job=256):
+def _sweep_jobs(mq, ions_per_job=256, seed0=0):
     fac = np.linspace(80e3, 120e3, 64)
     vac = np.linspace(0.1, 1.0, 8)
     mzs = [470.0 + 2 * k for k in range(32)]
@@ -27,7 +28,7 @@ def _sweep_jobs(mq, ions_per_job=256):
         for v in vac:
             for m in mzs:
                 jobs.append(mq.Job(mq.Species(m, 1.0, 2.95 * m ** (2.0 / 3.0)), mq.RfAc(100.0, 500e3, float(v), float(a)),
-                                   ions_per_job, len(jobs)))
+                                   ions_per_job, seed0 + len(jobs)))
     ph = mq.Physics(legacy_force=True, pressure_pa=0.133322, temp_k=300.0, dt=1e-7, t_max=20000 * 1e-7,
                     launch=mq.LAUNCH_GAUSSIAN, sigma_mm=0.1, z_inject_mm=1.0)
     return jobs, ph, [0.0, 5.0, -5.0, 0.0]
@@ -72,6 +73,31 @@ def test_full_sweep_properties(grid_0p1):
     from multiq_workbench_gb300 import validate as V
     r = V.compare_classes(V.class_counts(om), V.class_counts(o64))
     print(f"\nPARITY config 2 (16 ions of each of the 16,384 jobs): chi2 {r['chi2']:.2f} dof {r['dof']} p {r['p']:.3f}; "
+          + ", ".join(f"{k} {c['a']}/{c['b']} ({c['pull']:+.2f})" for k, c in r["classes"].items()))
+    assert r["p"] >= 0.05, r
+
+
+def test_full_sweep_counts_at_four_seed_sets(grid_0p1):
+    """The whole batch (4,194,304 ions) on both kernels at four seed sets (job seeds offset by 0, 1e6,
+    2e6, 3e6): the mixed engine's outcome-class totals over the four sets match the FP64 kernel's at
+    the 95% level (one chi-square over the classes of the pooled 16.8 M ions; each set's own p is
+    printed, and with four sets a single one below 0.05 is expected one time in five)."""
+    import multiq_workbench_gb300 as mq
+    from multiq_workbench_gb300 import validate as V
+    tot_m, tot_64, per_set = None, None, []
+    for seed0 in (0, 1_000_000, 2_000_000, 3_000_000):
+        jobs, ph, dc = _sweep_jobs(mq, seed0=seed0)
+        table = mq.JobTable.from_jobs(jobs)
+        with mq.Engine(grid_0p1, mq.PREC_MIXED) as e:
+            cm = V.class_counts(e.run_batch(table, dc, ph))
+        with mq.Engine(grid_0p1, mq.PREC_F64) as e64:
+            c64 = V.class_counts(e64.run_batch(table, dc, ph))
+        per_set.append(V.compare_classes(cm, c64)["p"])
+        tot_m = cm if tot_m is None else {k: tot_m[k] + cm[k] for k in cm}
+        tot_64 = c64 if tot_64 is None else {k: tot_64[k] + c64[k] for k in c64}
+    r = V.compare_classes(tot_m, tot_64)
+    print(f"\nPARITY config 2, whole batch at four seed sets: chi2 {r['chi2']:.2f} dof {r['dof']} p {r['p']:.3f} "
+          f"(per set {' / '.join(f'{q:.2f}' for q in per_set)}); "
           + ", ".join(f"{k} {c['a']}/{c['b']} ({c['pull']:+.2f})" for k, c in r["classes"].items()))
     assert r["p"] >= 0.05, r
 
