@@ -829,12 +829,12 @@ Tuning default_tuning(int device, size_t nodes) {
     t.sms = sms;
     // Resident ions per SM by the size of the node records: on grids far larger than L2 the
     // gathers of fewer ions in flight hit the caches more often than more warps hide latency
-    // (measured on the channel at 0.100 / 0.050 / 0.0333 mm, 0.30 / 2.4 / 8.0 GB of 48-byte
-    // records: best at 3 / 2 / 1 blocks per SM, 28.7 / 17.9 / 9.8 G ion-steps/s against
-    // 28.7 / 11.1 / 6.4 with 3 everywhere). Wide records only in the first class: they win where
-    // the reloads hit L2 and lose where they reach HBM.
+    // (measured on the channel at 0.050 / 0.0333 mm, 2.4 / 8.0 GB of 48-byte records: 15.7 / 11.4
+    // G ion-steps/s at 1 block per SM against 15.0 / 7.1 at 2 and 10.6 / - at 3; the 0.100 mm grid,
+    // 0.30 GB, is best at 3). Wide records only in the first class: they win where the reloads hit
+    // L2 and lose where they reach HBM.
     const double rec = 48.0 * (double)nodes;
-    t.blocks_per_sm = rec < 1.0e9 ? 3 : (rec < 4.0e9 ? 2 : 1);
+    t.blocks_per_sm = rec < 1.0e9 ? 3 : 1;
     t.wide = rec < 1.0e9 ? 1 : 0;
     return t;
 }

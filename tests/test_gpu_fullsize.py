@@ -137,14 +137,14 @@ def test_full_tandem_properties(built):
 
 def test_default_shape_follows_the_grid_size(built):
     """Fewer resident blocks per SM on grids far larger than L2 (node records of 0.30 / 2.4 /
-    8.0 GB at 0.100 / 0.050 / 0.0333 mm give 3 / 2 / 1), and each shape runs the grid-study
+    8.0 GB at 0.100 / 0.050 / 0.0333 mm give 3 / 1 / 1), and each shape runs the grid-study
     launch to completion."""
     import multiq_workbench_gb300 as mq
     ph = mq.Physics(legacy_force=True, pressure_pa=0.133322, temp_k=300.0, dt=1e-7, t_max=2000 * 1e-7,
                     launch=mq.LAUNCH_GAUSSIAN, sigma_mm=0.1)
     jobs = [mq.Job(mq.Species(499.0, 1.0, 2.95 * 499.0 ** (2 / 3)), mq.RfAc(100.0, 500e3, 0.5, 100e3), 1000, s)
             for s in range(8)]
-    for h, want in ((0.05, 2), (0.1 / 3.0, 1)):
+    for h, want in ((0.05, 1), (0.1 / 3.0, 1)):
         f = mq.Fields.build(mq.Geom.with_spacing(h), bases=[0, 1, 3, 4], cache=False, device=0)
         with mq.Engine(f, mq.PREC_MIXED) as e:
             assert e.tuning()["blocks_per_sm"] == want, h
