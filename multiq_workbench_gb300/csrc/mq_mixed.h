@@ -12,7 +12,7 @@ struct MixJob {
     float kick;        // qm_kick * dt * dt / h
     float v_ac;        // AC amplitude [V]
     float cand_a;      // null-collision candidate probability per |u| (nsd * h / dt)
-    float cand_b;      //   ... constant part (nsd * 6 s_gas)
+    float cand_b;      //   ... constant part (nsd * E|V|, E|V| = 2 sqrt(2/pi) s_gas: mqx::thermal_partner)
     float s_gas;       // Maxwell gas std [m/s]
     float mr;          // M_gas / (m + M_gas)
     float floor_v;     // legacy: no collision below this speed [m/s]; < 0 = thermal gas
