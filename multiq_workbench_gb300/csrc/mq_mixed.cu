@@ -384,8 +384,12 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
                 }
                 if ((n & 3) == 0) rc = rn;   // rn holds block n>>2: refreshed at most 3 iterations ago
             } else {
+                // a collision is due every ~4 steps per ion, so some lane of the warp needs one on
+                // almost every iteration: every lane computes it and keeps it only where it is due,
+                // with selects instead of a divergent branch
                 leg -= 1;
-                if (leg <= 0) {
+                const bool due = leg <= 0;
+                {
                     const float mr = sj_mr[threadIdx.x], floor_v = sj_floor[threadIdx.x], mfp_mean = sj_mfp[threadIdx.x];
                     // two 32-bit words of this window step: cos(theta) from the top 24 bits of the
                     // first, the free path from the top 24 of the second, phi from their low bytes
@@ -395,27 +399,29 @@ k_mixed(const float4* __restrict__ nodes, MixBatch B, const MixJob* __restrict__
                     const float u2v = B.u2v_f;
                     float v[3] = {uh[0] * u2v, uh[1] * u2v, uh[2] * u2v};
                     const float vm = sqrtf(fmaf(v[0], v[0], fmaf(v[1], v[1], v[2] * v[2])));
-                    if (vm > floor_v) {
-                        const float cth = 2.0f * unif(wa) - 1.0f;
-                        float sp, cp;
-                        angle_sincos(unif16(((wa & 0xffu) << 8) | (wb & 0xffu)), &sp, &cp);
-                        const float sn = sqrtf(fmaxf(0.0f, 1.0f - cth * cth));
-                        const float dd[3] = {sn * cp, sn * sp, cth};
-                        const float v2u = B.v2u_f;
+                    const bool hit = due && vm > floor_v;
+                    const float cth = 2.0f * unif(wa) - 1.0f;
+                    float sp, cp;
+                    angle_sincos(unif16(((wa & 0xffu) << 8) | (wb & 0xffu)), &sp, &cp);
+                    const float sn = sqrtf(fmaxf(0.0f, 1.0f - cth * cth));
+                    const float dd[3] = {sn * cp, sn * sp, cth};
+                    const float v2u = B.v2u_f;
 #pragma unroll
-                        for (int d = 0; d < 3; ++d) {
-                            v[d] = fmaf(mr * vm, dd[d], v[d] * (1.0f - mr));
-                            uh[d] = v[d] * v2u; ul[d] = 0.0f;
-                        }
-                        ncoll += 1;
+                    for (int d = 0; d < 3; ++d) {
+                        const float vn = fmaf(mr * vm, dd[d], v[d] * (1.0f - mr));
+                        v[d] = hit ? vn : v[d];
+                        uh[d] = hit ? vn * v2u : uh[d];
+                        ul[d] = hit ? 0.0f : ul[d];
                     }
+                    ncoll += hit ? 1u : 0u;
                     const float mfp = -__logf(fmaxf(unif(wb), 1e-7f)) * mfp_mean;
                     const float vn = sqrtf(fmaf(v[0], v[0], fmaf(v[1], v[1], v[2] * v[2])));
                     // free path in steps with the hardware's approximate division (within 2 ulp; the
                     // floored count moves by one step in rare ties, a few ions in 10^5; 3.8% on the
                     // legacy scan against two IEEE divisions)
                     const float st = floorf(__fdividef(mfp, fmaxf(vn, 1e-3f) * B.dt_f));
-                    leg = st < 1.0f ? 1 : (st < 2147483520.0f ? (int32_t)st : 2147483647);
+                    const int32_t nl = st < 1.0f ? 1 : (st < 2147483520.0f ? (int32_t)st : 2147483647);
+                    leg = due ? nl : leg;
                 }
             }
             // ---- cell of the new position (refresh the cache before the conductor test), and
