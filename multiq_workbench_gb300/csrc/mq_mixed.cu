@@ -19,7 +19,7 @@
 //   * Philox-4x32-10 counter RNG keyed by the ion's 64-bit key, counter = step (thermal candidates
 //     and collisions) or 4-step window (legacy collisions: two blocks per window); thermal
 //     candidates drawn against the majorant |v| + E|V| (mqx::thermal_partner), which samples the
-//     reference's collision process with 2-4 times fewer candidates than its |v| + 6 s_gas;
+//     reference's collision process with 2 to 3.4 times fewer candidates than its |v| + 6 s_gas;
 //   * device injection with the FP64 injection's draws and FP32 transforms (k_inject_mixed).
 #include "mq_mixed.h"
 #include "mq_check.h"

@@ -37,10 +37,10 @@ __device__ __forceinline__ void angle_sincos(float u, float* s, float* c) { __si
 // |v - V| / (|v| + |V|) <= 1 (triangle inequality). The accepted rate density is
 // n sigma (|v| + E|V|) q(V) |v - V| / (|v| + |V|) = n sigma f(V) |v - V|: the same collision process,
 // exactly (a gas speed above 6 s, about 1e-7 of the draws, can exceed the 6 s bound; this bound
-// holds for every draw), with a candidate rate 2-4 times smaller for the ions of these engines. q is a two-part mixture: with
-// probability |v| / (|v| + E|V|) the Maxwellian f itself (Box-Muller), else the speed-weighted
-// Maxwellian |V| f(V) / E|V|, whose speed r has r^2 / 2 s^2 ~ Gamma(2, 1) = -ln(u1 u2) and whose
-// direction is uniform. Uses from r: x, y (24-bit uniforms of the radii), z (two 16-bit angles or
+// holds for every draw), with a candidate rate 2 to 3.4 times smaller (ion speeds from 3 s down to
+// 0.2 s). q is a two-part mixture: with probability |v| / (|v| + E|V|) the Maxwellian f itself
+// (Box-Muller), else the speed-weighted Maxwellian |V| f(V) / E|V|, whose speed r has
+// r^2 / 2 s^2 ~ Gamma(2, 1) = -ln(u1 u2) and whose direction is uniform. Uses from r: x, y (24-bit uniforms of the radii), z (two 16-bit angles or
 // cos theta and an angle), w >> 16 (the mixture choice); w & 0xffff is left for the acceptance.
 constexpr float kMeanSpeed = 1.59576912f;   // E|V| / s = 2 sqrt(2 / pi)
 

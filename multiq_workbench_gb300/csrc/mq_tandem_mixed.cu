@@ -20,7 +20,7 @@
 //     collisions with Philox-4x32-10 keyed by the track key and the global step (all lanes
 //     share the global step, so the generator runs warp-uniformly), their candidates drawn
 //     against the majorant |v| + E|V| of mqx::thermal_partner (the reference's |v| + 6 s_gas
-//     samples the same process with 2-4 times as many candidates);
+//     samples the same process with 2 to 3.4 times as many candidates);
 //   * cube losses by the geometry test in FP32, skipped in the interior box where every
 //     face is farther than the post tops (geometry.rs:166 makes such points free).
 #include <cmath>
